@@ -1,0 +1,166 @@
+"""ctypes binding of libfsg.so (the C ABI in include/fsg.h).
+
+The library is built in-tree by ``fake_spectra_gb300.build.build()``.  There is
+no CPU fallback: if the library is missing, loading raises.
+"""
+import ctypes
+import os
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libfsg.so")
+
+FSG_OK = 0
+FSG_ERR_VALUE = 1
+FSG_ERR_TYPE = 2
+FSG_ERR_MEMORY = 3
+FSG_ERR_CUDA = 4
+FSG_ERR_NOT_IMPLEMENTED = 5
+FSG_ERR_DEVICE = 6
+
+FSG_PREC_FP64 = 0
+FSG_PREC_FP32 = 1
+
+# Names exported by libfsg.so, one per declaration in include/fsg.h.
+EXPORTS = (
+    "fsg_version",
+    "fsg_context_create",
+    "fsg_context_destroy",
+    "fsg_context_set_stream",
+    "fsg_context_stats",
+    "fsg_particle_interpolate",
+    "fsg_particle_interpolate_device",
+    "fsg_build_pairs_device",
+    "fsg_copy_pairs",
+)
+
+_c_int = ctypes.c_int
+_c_i64 = ctypes.c_int64
+_c_i32 = ctypes.c_int32
+_c_d = ctypes.c_double
+_p = ctypes.c_void_p
+_c_size = ctypes.c_size_t
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", _c_int), ("threads", _c_int), ("persistent", _c_int),
+                ("reserved", _c_int * 5)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("npairs", _c_i64), ("gpu_launches", _c_i64), ("fallback_lines", _c_i32),
+                ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d)]
+
+
+class FsgError(RuntimeError):
+    """A CUDA-side failure reported by libfsg."""
+
+
+class FsgDeviceError(FsgError):
+    """A kernel reported an internal limit (FSG_ERR_DEVICE)."""
+
+
+def raise_for(code, msg):
+    """Map an fsg_status to the exception class the reference raises."""
+    if code == FSG_OK:
+        return
+    text = msg or "fsg error %d" % code
+    if code == FSG_ERR_VALUE:
+        raise ValueError(text)
+    if code == FSG_ERR_TYPE:
+        raise TypeError(text)
+    if code == FSG_ERR_MEMORY:
+        raise MemoryError(text)
+    if code == FSG_ERR_NOT_IMPLEMENTED:
+        raise NotImplementedError(text)
+    if code == FSG_ERR_DEVICE:
+        raise FsgDeviceError(text)
+    raise FsgError(text)
+
+
+_lib = None
+_lock = threading.Lock()
+
+_INTERP_ARGS = [_c_int, _c_int, _c_int] + [_c_d] * 8 + [_p] * 5 + [_c_i64, _p, _p, _c_i32, _p,
+                                                                     _p, _p, _c_size]
+
+
+def load(path=None):
+    """Load libfsg.so (once).  Raises if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            raise ImportError("libfsg.so is not built (%s); run "
+                              "fake_spectra_gb300.build.build() on a machine with nvcc" % path)
+        L = ctypes.CDLL(path)
+        L.fsg_version.restype = ctypes.c_char_p
+        L.fsg_context_create.argtypes = [_c_int, ctypes.POINTER(_p), _p, _c_size]
+        L.fsg_context_destroy.argtypes = [_p]
+        L.fsg_context_destroy.restype = None
+        L.fsg_context_set_stream.argtypes = [_p, _p]
+        L.fsg_context_stats.argtypes = [_p, ctypes.POINTER(Stats)]
+        L.fsg_particle_interpolate.argtypes = _INTERP_ARGS
+        L.fsg_particle_interpolate_device.argtypes = [_p] + _INTERP_ARGS
+        L.fsg_build_pairs_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32,
+                                             ctypes.POINTER(_c_i64), _p, _c_size]
+        L.fsg_copy_pairs.argtypes = [_p, _p, _p, _p, _c_int, _p, _c_size]
+        _lib = L
+        return L
+
+
+def errbuf():
+    return ctypes.create_string_buffer(512)
+
+
+def make_options(precision="fp64", threads=0, persistent=-1):
+    o = Options()
+    if precision in ("fp64", FSG_PREC_FP64):
+        o.precision = FSG_PREC_FP64
+    elif precision in ("fp32", FSG_PREC_FP32):
+        o.precision = FSG_PREC_FP32
+    else:
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    o.threads = int(threads)
+    o.persistent = int(persistent)
+    return o
+
+
+class Context:
+    """An fsg_context: one device, one stream, a cached device workspace."""
+
+    def __init__(self, device=0):
+        L = load()
+        h = _p()
+        eb = errbuf()
+        raise_for(L.fsg_context_create(int(device), ctypes.byref(h), eb, 512), eb.value.decode())
+        self._h = h
+        self._lib = L
+        self.device = int(device)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        self._lib.fsg_context_set_stream(self._h, _p(stream_ptr) if stream_ptr else None)
+
+    def stats(self):
+        s = Stats()
+        self._lib.fsg_context_stats(self._h, ctypes.byref(s))
+        return {"npairs": int(s.npairs), "gpu_launches": int(s.gpu_launches),
+                "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
+                "ms_deposit": float(s.ms_deposit)}
+
+    def close(self):
+        if self._h:
+            self._lib.fsg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

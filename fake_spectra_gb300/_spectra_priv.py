@@ -1,0 +1,114 @@
+"""Drop-in replacement for the reference extension module ``fake_spectra._spectra_priv``.
+
+``_Particle_Interpolate`` keeps the reference's positional arguments, argument
+checks, exception classes and return value (py_module.cpp:103-233,
+Py_Particle_Interpolation): a new float64 array of shape (NumLos, nbins)
+holding tau (compute_tau=1) or the column density (compute_tau=0).  The work
+runs on the GPU through libfsg's C ABI; there is no CPU path.
+
+Differences from the reference, all for inputs on which the reference has
+undefined behaviour: axis values outside {1, 2, 3}, non-finite sightline
+positions, pos/vel arrays that are not (Npart, 3), and a non-positive box size
+raise ValueError; the Voronoi kernel (kernel=2) raises NotImplementedError.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_ATTR_MSG = ("Incorrect arguments: use compute_tau, nbins, boxsize, velfac, atime, lambda, gamma, "
+             "fosc, species mass (amu), min. tau,  pos, vel, dens, temp, h, axis, cofm\n")
+
+
+def _as_int(v):
+    # PyArg_ParseTuple "i": integers (or __index__), not floats
+    if isinstance(v, (bool, int, np.integer)):
+        return int(v)
+    if isinstance(v, (float, np.floating)):
+        raise AttributeError(_ATTR_MSG)
+    try:
+        return int(v.__index__())
+    except Exception:
+        raise AttributeError(_ATTR_MSG) from None
+
+
+def _as_float(v):
+    # "d": floats or integers
+    try:
+        return float(v)
+    except Exception:
+        raise AttributeError(_ATTR_MSG) from None
+
+
+def _to_numpy(a):
+    if isinstance(a, np.ndarray):
+        return a
+    # torch tensors are accepted as well (moved to host memory)
+    if hasattr(a, "detach") and hasattr(a, "cpu") and hasattr(a, "numpy"):
+        return a.detach().cpu().numpy()
+    raise AttributeError(_ATTR_MSG)
+
+
+def check_arrays(compute_tau, pos, vel, dens, temp, h, axis, cofm):
+    """The dtype and shape checks of py_module.cpp:121-151, in the same order."""
+    for a in (pos, vel, dens, temp, h):
+        if a.dtype != np.float32:
+            raise TypeError("One of the data arrays does not have 32-bit float type\n")
+    if cofm.dtype != np.float64:
+        raise TypeError("Sightline positions must have 64-bit float type\n")
+    if axis.dtype != np.int32:
+        raise TypeError("Axis must be a 32-bit integer\n")
+    npart = pos.shape[0] if pos.ndim >= 1 else 0
+    if dens.ndim < 1 or h.ndim < 1 or npart != dens.shape[0] or npart != h.shape[0]:
+        raise ValueError(" Dens, pos and h must have the same length\n")
+    if cofm.ndim != 2 or axis.ndim < 1 or cofm.shape[0] != axis.shape[0] or cofm.shape[1] != 3:
+        raise ValueError("cofm must have dimensions (np.size(axis),3) \n")
+    if pos.ndim != 2 or pos.shape[1] != 3:
+        raise ValueError("pos must have dimensions (Npart, 3)\n")
+    if compute_tau:
+        if vel.ndim != 2 or vel.shape[0] != npart or vel.shape[1] != 3:
+            raise ValueError("vel must have dimensions (Npart, 3)\n")
+        if temp.ndim < 1 or temp.shape[0] != npart:
+            raise ValueError("temp must have the same length as dens\n")
+    return npart, int(axis.shape[0])
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1):
+    """tau or colden along every sightline; see the module docstring."""
+    if len(args) != 18:
+        raise AttributeError(_ATTR_MSG)
+    compute_tau, nbins, kernel = (_as_int(v) for v in args[:3])
+    box, velfac, atime, lam, gamma, fosc, amumass, tautail = (_as_float(v) for v in args[3:11])
+    pos, vel, dens, temp, h, axis, cofm = (_to_numpy(a) for a in args[11:18])
+    npart, nlos = check_arrays(compute_tau, pos, vel, dens, temp, h, axis, cofm)
+    if nbins < 0:
+        raise ValueError("negative dimensions are not allowed")
+    pos = np.ascontiguousarray(pos)
+    dens = np.ascontiguousarray(dens)
+    h = np.ascontiguousarray(h)
+    axis = np.ascontiguousarray(axis)
+    cofm = np.ascontiguousarray(cofm)
+    if compute_tau:
+        vel = np.ascontiguousarray(vel)
+        temp = np.ascontiguousarray(temp)
+    out = np.zeros((nlos, nbins), dtype=np.float64)
+    if nlos == 0 or nbins == 0:
+        if kernel == 2:
+            raise NotImplementedError("the Voronoi-mesh kernel (kernel == 2) is not implemented")
+        return out
+    L = _lib.load()
+    opt = _lib.make_options(precision, threads, persistent)
+    eb = _lib.errbuf()
+    rc = L.fsg_particle_interpolate(int(compute_tau), nbins, kernel, box, velfac, atime, lam,
+                                    gamma, fosc, amumass, tautail, _ptr(pos),
+                                    _ptr(vel) if compute_tau else None, _ptr(dens),
+                                    _ptr(temp) if compute_tau else None, _ptr(h), npart,
+                                    _ptr(axis), _ptr(cofm), nlos, _ptr(out), ctypes.byref(opt), eb,
+                                    512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return out

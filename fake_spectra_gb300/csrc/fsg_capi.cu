@@ -1,0 +1,574 @@
+// Host side of libfsg: the C ABI declared in include/fsg.h.
+//
+// Call pipeline (all on the context's stream):
+//   1. sightline tables: keys, second coordinates and one transverse cell grid
+//      per axis group, built on the host from axis/cofm (tiny) and uploaded;
+//   2. pair search: count kernel -> per-sightline totals -> host prefix sum
+//      (one small device->host copy, which also sizes the pair buffers) ->
+//      emit kernel writing CSR pair lists;
+//   3. deposit: sightlines ordered by descending pair count; one kernel;
+//      sightlines with non-finite contributions re-run by the fallback kernel.
+#include "fsg.h"
+#include "fsg_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using namespace fsg;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+// Thrown internally and turned into a status at the API boundary.
+struct FsgError {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw FsgError{code, buf};
+}
+
+void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation)
+            fail(FSG_ERR_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+        fail(FSG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+}
+
+int report(const FsgError &e, char *errbuf, size_t errlen)
+{
+    if (errbuf && errlen) {
+        strncpy(errbuf, e.msg.c_str(), errlen - 1);
+        errbuf[errlen - 1] = '\0';
+    }
+    return e.code;
+}
+
+}  // namespace
+
+struct fsg_context {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    // workspace
+    DevBuf pos, vel, dens, temp, hh, out;                    // staging for host-pointer calls
+    DevBuf key, second, axis, cell_start[3], cell_line[3];   // sightline tables
+    DevBuf line_count, cursor, off, part, dr2, line_order;   // pair lists
+    DevBuf ticket, bad, nbad, err, gacc;                     // deposit bookkeeping
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // host mirrors
+    std::vector<long long> h_off;
+    std::vector<int> h_order;
+    int nlos = 0;
+    long long npairs = 0;
+    LineTables tables{};
+    fsg_stats stats{};
+
+    void *ensure(DevBuf &b, size_t bytes)
+    {
+        if (bytes == 0)
+            bytes = 16;
+        if (b.cap < bytes) {
+            if (b.p)
+                cuda_check(cudaFree(b.p), "cudaFree");
+            b.p = nullptr;
+            b.cap = 0;
+            size_t want = bytes + bytes / 8;
+            cuda_check(cudaMalloc(&b.p, want), "cudaMalloc");
+            b.cap = want;
+        }
+        return b.p;
+    }
+
+    void release_all()
+    {
+        DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis,
+                          &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
+                          &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
+                          &line_order, &ticket, &bad, &nbad, &err, &gacc};
+        for (DevBuf *b : bufs) {
+            if (b->p)
+                cudaFree(b->p);
+            b->p = nullptr;
+            b->cap = 0;
+        }
+    }
+};
+
+namespace {
+
+void validate_common(int nbins, int kernel, double box, int64_t npart, int32_t nlos,
+                     const int32_t *axis, const double *cofm)
+{
+    if (nbins < 0)
+        fail(FSG_ERR_VALUE, "nbins must be non-negative (got %d)", nbins);
+    if (npart < 0 || nlos < 0)
+        fail(FSG_ERR_VALUE, "negative array length");
+    if (npart > 2147483647LL)
+        fail(FSG_ERR_VALUE, "at most 2^31-1 particles (particle indices are int, as in the "
+                            "reference's std::map<int, double>)");
+    if (kernel == VORONOI)
+        fail(FSG_ERR_NOT_IMPLEMENTED, "the Voronoi-mesh kernel (kernel == 2) is not implemented");
+    if (!(box > 0.0) || !std::isfinite(box))
+        fail(FSG_ERR_VALUE, "box size must be positive and finite (got %g)", box);
+    for (int i = 0; i < nlos; i++) {
+        if (axis[i] < 1 || axis[i] > 3)
+            fail(FSG_ERR_VALUE, "axis[%d] = %d: sightline axes must be 1, 2 or 3", i, axis[i]);
+        for (int k = 0; k < 3; k++)
+            if (!std::isfinite(cofm[3 * (size_t)i + k]))
+                fail(FSG_ERR_VALUE, "cofm[%d] is not finite", i);
+    }
+}
+
+// 1. sightline tables
+void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int nlos, double box)
+{
+    std::vector<double> key(nlos), second(nlos);
+    std::vector<int> grp_lines[3];
+    for (int i = 0; i < nlos; i++) {
+        const int a = axis[i];
+        key[i] = (a == 1) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i];
+        second[i] = (a == 3) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i + 2];
+        grp_lines[a - 1].push_back(i);
+    }
+    LineTables &t = c->tables;
+    t = LineTables{};
+    t.nlos = nlos;
+    t.box = box;
+    t.n_xx = (int)grp_lines[0].size();
+    t.n_main = nlos - t.n_xx;
+    cudaStream_t s = c->stream;
+    for (int g = 0; g < 3; g++) {
+        LineGroup &G = t.g[g];
+        const int n = (int)grp_lines[g].size();
+        G.nlines = n;
+        if (n == 0)
+            continue;
+        int nc = (int)std::ceil(std::sqrt((double)n));
+        nc = std::max(1, std::min(nc, 1024));
+        G.nc = nc;
+        G.cw = box / nc;
+        G.inv_cw = nc / box;
+        auto cell_of = [&](double v) {
+            double m = v - box * std::floor(v / box);
+            long long ci = (long long)std::floor(m * G.inv_cw);
+            return (int)std::min<long long>(std::max<long long>(ci, 0), nc - 1);
+        };
+        std::vector<int> cnt((size_t)nc * nc + 1, 0), cell(n);
+        for (int k = 0; k < n; k++) {
+            const int l = grp_lines[g][k];
+            cell[k] = cell_of(key[l]) * nc + cell_of(second[l]);
+            cnt[cell[k] + 1]++;
+        }
+        for (size_t k = 0; k < (size_t)nc * nc; k++)
+            cnt[k + 1] += cnt[k];
+        std::vector<int> lines(n), cur(cnt.begin(), cnt.end() - 1);
+        for (int k = 0; k < n; k++)
+            lines[cur[cell[k]]++] = grp_lines[g][k];
+        void *cs = c->ensure(c->cell_start[g], sizeof(int) * cnt.size());
+        void *cl = c->ensure(c->cell_line[g], sizeof(int) * n);
+        cuda_check(cudaMemcpyAsync(cs, cnt.data(), sizeof(int) * cnt.size(),
+                                   cudaMemcpyHostToDevice, s), "upload cells");
+        cuda_check(cudaMemcpyAsync(cl, lines.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s),
+                   "upload cells");
+        // the host vectors die at scope end: finish the copies first
+        cuda_check(cudaStreamSynchronize(s), "upload cells");
+        G.cell_start = (const int *)cs;
+        G.cell_line = (const int *)cl;
+    }
+    void *dk = c->ensure(c->key, sizeof(double) * nlos);
+    void *ds = c->ensure(c->second, sizeof(double) * nlos);
+    void *da = c->ensure(c->axis, sizeof(int) * nlos);
+    cuda_check(cudaMemcpyAsync(dk, key.data(), sizeof(double) * nlos, cudaMemcpyHostToDevice, s),
+               "upload sightlines");
+    cuda_check(cudaMemcpyAsync(ds, second.data(), sizeof(double) * nlos, cudaMemcpyHostToDevice,
+                               s), "upload sightlines");
+    cuda_check(cudaMemcpyAsync(da, axis, sizeof(int) * nlos, cudaMemcpyHostToDevice, s),
+               "upload sightlines");
+    cuda_check(cudaStreamSynchronize(s), "upload sightlines");
+    t.key = (const double *)dk;
+    t.second = (const double *)ds;
+    t.axis = (const int *)da;
+    c->nlos = nlos;
+}
+
+// 2. pair search
+void search_pairs(fsg_context *c, const Particles &p, int nlos)
+{
+    cudaStream_t s = c->stream;
+    cuda_check(cudaEventRecord(c->ev[0], s), "event");
+    auto *cnt = (unsigned long long *)c->ensure(c->line_count, sizeof(unsigned long long) * nlos);
+    cuda_check(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * nlos, s), "memset");
+    launch_count_pairs(c->tables, p, cnt, nullptr, s);
+    if (p.n > 0)
+        c->stats.gpu_launches++;
+    cuda_check(cudaGetLastError(), "count_pairs launch");
+    std::vector<unsigned long long> h_cnt(nlos);
+    cuda_check(cudaMemcpyAsync(h_cnt.data(), cnt, sizeof(unsigned long long) * nlos,
+                               cudaMemcpyDeviceToHost, s), "read counts");
+    cuda_check(cudaStreamSynchronize(s), "count_pairs");
+    c->h_off.assign((size_t)nlos + 1, 0);
+    for (int i = 0; i < nlos; i++)
+        c->h_off[i + 1] = c->h_off[i] + (long long)h_cnt[i];
+    const long long total = c->h_off[nlos];
+    c->npairs = total;
+    auto *off = (long long *)c->ensure(c->off, sizeof(long long) * (nlos + 1));
+    cuda_check(cudaMemcpyAsync(off, c->h_off.data(), sizeof(long long) * (nlos + 1),
+                               cudaMemcpyHostToDevice, s), "upload offsets");
+    auto *cur = (unsigned long long *)c->ensure(c->cursor, sizeof(unsigned long long) * nlos);
+    cuda_check(cudaMemsetAsync(cur, 0, sizeof(unsigned long long) * nlos, s), "memset");
+    int *part = (int *)c->ensure(c->part, sizeof(int) * total);
+    double *dr2 = (double *)c->ensure(c->dr2, sizeof(double) * total);
+    auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
+    cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
+    if (total > 0) {
+        launch_emit_pairs(c->tables, p, off, cur, part, dr2, err, s);
+        c->stats.gpu_launches++;
+        cuda_check(cudaGetLastError(), "emit_pairs launch");
+    }
+    // sightline work order: descending pair count (largest first)
+    c->h_order.resize(nlos);
+    std::iota(c->h_order.begin(), c->h_order.end(), 0);
+    std::stable_sort(c->h_order.begin(), c->h_order.end(),
+                     [&](int a, int b) { return h_cnt[a] > h_cnt[b]; });
+    void *ord = c->ensure(c->line_order, sizeof(int) * nlos);
+    cuda_check(cudaMemcpyAsync(ord, c->h_order.data(), sizeof(int) * nlos,
+                               cudaMemcpyHostToDevice, s), "upload order");
+    cuda_check(cudaEventRecord(c->ev[1], s), "event");
+    unsigned h_err = 0;
+    cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "emit_pairs");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    c->stats.ms_search = ms;
+    c->stats.npairs = total;
+    if (h_err)
+        fail(FSG_ERR_DEVICE, "pair search reported device error bits 0x%x", h_err);
+}
+
+// 3. deposit into out (device, nlos*nbins)
+void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
+             const fsg_options *opt)
+{
+    cudaStream_t s = c->stream;
+    const int nlos = c->nlos;
+    const size_t nout = (size_t)nlos * lp.nbins;
+    cuda_check(cudaEventRecord(c->ev[2], s), "event");
+    if (nout)
+        cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * nout, s), "memset out");
+    c->stats.fallback_lines = 0;
+    if (nout == 0 || c->npairs == 0) {
+        cuda_check(cudaEventRecord(c->ev[3], s), "event");
+        cuda_check(cudaStreamSynchronize(s), "deposit");
+        c->stats.ms_deposit = 0;
+        return;
+    }
+    PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
+    DepositLaunch cfg{};
+    cfg.precision = opt ? opt->precision : FSG_PREC_FP64;
+    cfg.threads = (opt && opt->threads > 0) ? opt->threads : 256;
+    cfg.smem_mode = lp.nbins <= deposit_max_smem_bins();
+    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent : 0;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    cfg.grid = std::min(nlos, sms * 2);
+    unsigned long long *gacc = nullptr;
+    if (!cfg.smem_mode) {
+        gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
+    }
+    auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
+    auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
+    auto *nbad = (int *)c->ensure(c->nbad, sizeof(int));
+    auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
+    cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
+    cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int), s), "memset");
+    cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
+    launch_deposit(lp, c->tables, p, pl, (const int *)c->line_order.p, nlos, out, ticket, bad,
+                   nbad, err, gacc, cfg, s);
+    c->stats.gpu_launches++;
+    cuda_check(cudaGetLastError(), "deposit launch");
+    int h_nbad = 0;
+    unsigned h_err = 0;
+    cuda_check(cudaMemcpyAsync(&h_nbad, nbad, sizeof(int), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "deposit");
+    if (h_nbad > 0) {
+        launch_deposit_fallback(lp, c->tables, p, pl, bad, h_nbad, out, err, s);
+        c->stats.gpu_launches++;
+        cuda_check(cudaGetLastError(), "fallback launch");
+    }
+    c->stats.fallback_lines = h_nbad;
+    cuda_check(cudaEventRecord(c->ev[3], s), "event");
+    cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "deposit");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    c->stats.ms_deposit = ms;
+    if (h_err)
+        fail(FSG_ERR_DEVICE, "deposit kernel reported device error bits 0x%x", h_err);
+}
+
+LineParams make_line_params(int compute_tau, int nbins, int kernel, double box, double velfac,
+                            double lambda, double gamma, double fosc, double amumass,
+                            double tautail)
+{
+    // absorption.cpp:152-161 (constants absorption.cpp:21-33, absorption.h:4)
+    const double PI_D = 3.14159265358979323846;
+    const double SIGMA_T = 6.652458558e-25, BOLTZMANN = 1.3806504e-16;
+    const double PROTONMASS = 1.67262178e-24;
+    LineParams lp;
+    lp.compute_tau = compute_tau ? 1 : 0;
+    lp.nbins = nbins;
+    lp.kernel = kernel;
+    lp.tautail = tautail;
+    lp.sigma_a = std::sqrt(3.0 * PI_D * SIGMA_T / 8.0) * lambda * fosc;
+    lp.bfac = std::sqrt(2.0 * BOLTZMANN / (amumass * PROTONMASS)) / 1e5;
+    lp.voigt_fac = gamma * lambda / (4. * PI_D) / 1e5;
+    lp.velfac = velfac;
+    lp.vbox = box * velfac;
+    lp.box = box;
+    return lp;
+}
+
+fsg_context *g_default[64] = {nullptr};
+std::mutex g_default_mu;
+
+void ctx_init(fsg_context *c, int device)
+{
+    c->device = device;
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    cuda_check(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
+    c->stream = c->own;
+    for (auto &e : c->ev)
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+}
+
+void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, double box,
+                     double velfac, double lambda, double gamma, double fosc, double amumass,
+                     double tautail, const Particles &p, const int32_t *axis, const double *cofm,
+                     int32_t nlos, double *out, const fsg_options *opt)
+{
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    build_tables(c, axis, cofm, nlos, box);
+    search_pairs(c, p, nlos);
+    LineParams lp = make_line_params(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                                     amumass, tautail);
+    deposit(c, lp, p, out, opt);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fsg_version(void) { return "fsg 0.1 (sm_103a)"; }
+
+int fsg_context_create(int device, fsg_context **ctx, char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        auto *c = new fsg_context();
+        try {
+            ctx_init(c, device);
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        *ctx = c;
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+void fsg_context_destroy(fsg_context *ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    ctx->release_all();
+    for (auto &e : ctx->ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (ctx->own)
+        cudaStreamDestroy(ctx->own);
+    delete ctx;
+}
+
+int fsg_context_set_stream(fsg_context *ctx, void *cuda_stream)
+{
+    if (!ctx)
+        return FSG_ERR_VALUE;
+    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own;
+    return FSG_OK;
+}
+
+int fsg_context_stats(const fsg_context *ctx, fsg_stats *out)
+{
+    if (!ctx || !out)
+        return FSG_ERR_VALUE;
+    *out = ctx->stats;
+    return FSG_OK;
+}
+
+int fsg_particle_interpolate_device(fsg_context *ctx, int compute_tau, int nbins, int kernel,
+                                    double box, double velfac, double atime, double lambda,
+                                    double gamma, double fosc, double amumass, double tautail,
+                                    const float *pos, const float *vel, const float *dens,
+                                    const float *temp, const float *h, int64_t npart,
+                                    const int32_t *axis, const double *cofm, int32_t nlos,
+                                    double *out, const fsg_options *opt, char *errbuf,
+                                    size_t errlen)
+{
+    (void)atime;   // stored but unused by the reference (absorption.cpp:157)
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        Particles p{pos, vel, dens, temp, h, (long long)npart};
+        run_interpolate(ctx, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                        amumass, tautail, p, axis, cofm, nlos, out, opt);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box, double velfac,
+                             double atime, double lambda, double gamma, double fosc,
+                             double amumass, double tautail, const float *pos, const float *vel,
+                             const float *dens, const float *temp, const float *h, int64_t npart,
+                             const int32_t *axis, const double *cofm, int32_t nlos, double *out,
+                             const fsg_options *opt, char *errbuf, size_t errlen)
+{
+    (void)atime;
+    try {
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        int dev = 0;
+        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        if (dev < 0 || dev >= 64)
+            fail(FSG_ERR_VALUE, "device ordinal %d out of range", dev);
+        fsg_context *c;
+        std::lock_guard<std::mutex> lock(g_default_mu);
+        if (!g_default[dev]) {
+            c = new fsg_context();
+            try {
+                ctx_init(c, dev);
+            } catch (...) {
+                delete c;
+                throw;
+            }
+            g_default[dev] = c;
+        }
+        c = g_default[dev];
+        cudaStream_t s = c->stream;
+        const size_t n3 = sizeof(float) * 3 * (size_t)npart, n1 = sizeof(float) * (size_t)npart;
+        auto up = [&](DevBuf &b, const void *src, size_t bytes) -> const float * {
+            void *d = c->ensure(b, bytes);
+            if (bytes)
+                cuda_check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s), "H2D");
+            return (const float *)d;
+        };
+        Particles p;
+        p.n = npart;
+        p.pos = up(c->pos, pos, n3);
+        p.dens = up(c->dens, dens, n1);
+        p.hh = up(c->hh, h, n1);
+        p.vel = compute_tau ? up(c->vel, vel, n3) : nullptr;
+        p.temp = compute_tau ? up(c->temp, temp, n1) : nullptr;
+        const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
+        double *dout = (double *)c->ensure(c->out, nout);
+        run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
+                        tautail, p, axis, cofm, nlos, dout, opt);
+        if (nout)
+            cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaStreamSynchronize(s), "D2H");
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const float *h,
+                           int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
+                           int64_t *npairs, char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        validate_common(0, SPH_CUBIC, box, npart, nlos, axis, cofm);
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        build_tables(ctx, axis, cofm, nlos, box);
+        Particles p{pos, nullptr, nullptr, nullptr, h, (long long)npart};
+        search_pairs(ctx, p, nlos);
+        if (npairs)
+            *npairs = ctx->npairs;
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr2, int sorted,
+                   char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        const int nlos = ctx->nlos;
+        const long long total = ctx->npairs;
+        for (int i = 0; i <= nlos; i++)
+            offsets[i] = ctx->h_off[i];
+        if (total > 0) {
+            cuda_check(cudaMemcpyAsync(part, ctx->part.p, sizeof(int) * total,
+                                       cudaMemcpyDeviceToHost, ctx->stream), "D2H pairs");
+            cuda_check(cudaMemcpyAsync(dr2, ctx->dr2.p, sizeof(double) * total,
+                                       cudaMemcpyDeviceToHost, ctx->stream), "D2H pairs");
+            cuda_check(cudaStreamSynchronize(ctx->stream), "D2H pairs");
+        }
+        if (sorted) {
+            std::vector<std::pair<int, double>> tmp;
+            for (int i = 0; i < nlos; i++) {
+                const long long a = offsets[i], b = offsets[i + 1];
+                tmp.resize(b - a);
+                for (long long k = a; k < b; k++)
+                    tmp[k - a] = {part[k], dr2[k]};
+                std::sort(tmp.begin(), tmp.end(),
+                          [](const std::pair<int, double> &x, const std::pair<int, double> &y) {
+                              return x.first < y.first;
+                          });
+                for (long long k = a; k < b; k++) {
+                    part[k] = tmp[k - a].first;
+                    dr2[k] = tmp[k - a].second;
+                }
+            }
+        }
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,278 @@
+// Sightline-particle search on the GPU: the replacement for the reference
+// IndexTable (fake_spectra/index_table.cpp:7-150).
+//
+// One thread per particle enumerates, for every axis group of sightlines, the
+// transverse grid cells that can hold a sightline within its smoothing length
+// (periodic, minimum image, plus a safety margin), and evaluates the
+// reference's own accept predicate on every candidate with the reference's
+// float/double arithmetic, operation by operation, with no FMA contraction
+// (explicit __fadd_rn / __dmul_rn / __dadd_rn):
+//   * the first-coordinate window [ffm, ffp) of index_table.cpp:89-113,
+//     computed in float and compared against the double multimap key, with
+//     the periodic wrap that splits the range in two;
+//   * second_close, index_table.cpp:52-68 (float window, double compare);
+//   * calc_dr2, index_table.cpp:70-87 (double minimum-image distance), and the
+//     accept test dr2 <= hh*hh with hh*hh a float product (index_table.cpp:45).
+// The cell walk is only a superset generator, so the accepted pair set and
+// every dr2 bit equal the reference's.  Degenerate smoothing lengths are
+// resolved exactly (see for_each_pair).
+//
+// Two passes: count (per-sightline totals) and emit (atomic slot per pair).
+#include "fsg_internal.cuh"
+
+namespace fsg {
+
+namespace {
+
+struct Window {   // first-coordinate window of one table for one particle
+    float ffm, ffp;
+    bool nowrap;
+};
+
+__device__ __forceinline__ Window make_window(float first, float hh, double box)
+{
+    Window w;
+    float ffp = __fadd_rn(first, hh);
+    if ((double)ffp > box)
+        ffp = (float)__dsub_rn((double)ffp, box);
+    float ffm = __fsub_rn(first, hh);
+    if (ffm < 0.0f)
+        ffm = (float)__dadd_rn((double)ffm, box);
+    w.ffm = ffm;
+    w.ffp = ffp;
+    w.nowrap = (ffm <= ffp);
+    return w;
+}
+
+__device__ __forceinline__ bool in_window(const Window &w, double key)
+{
+    // lower_bound(ffm) .. lower_bound(ffp) over the sorted keys (index_table.cpp:102-112)
+    if (w.nowrap)
+        return ((double)w.ffm <= key) && (key < (double)w.ffp);
+    return (key < (double)w.ffp) || (key >= (double)w.ffm);
+}
+
+__device__ __forceinline__ bool second_close(float second, double lproj2, float hh, double box)
+{
+    float ffp = __fadd_rn(second, hh);
+    if ((double)ffp > box)
+        if (lproj2 < __dsub_rn((double)ffp, box))
+            return true;
+    float ffm = __fsub_rn(second, hh);
+    if (ffm < 0.0f)
+        if (lproj2 > __dadd_rn((double)ffm, box))
+            return true;
+    return (lproj2 > (double)ffm) && (lproj2 < (double)ffp);
+}
+
+__device__ __forceinline__ double calc_dr2(double d1, double d2, double box)
+{
+    const double half = 0.5 * box;
+    double dr = fabs(d1);
+    if (dr > half)
+        dr = __dsub_rn(box, dr);
+    double dr2 = __dmul_rn(dr, dr);
+    dr = fabs(d2);
+    if (dr > half)
+        dr = __dsub_rn(box, dr);
+    return __dadd_rn(dr2, __dmul_rn(dr, dr));
+}
+
+// The reference predicate for (particle, line).  `first` is the particle's
+// coordinate for the table the line is in; pos3 the particle position.
+__device__ __forceinline__ bool accept(const LineTables &t, int line, const Window &w,
+                                       float first, const float *pos3, float hh, double *dr2_out)
+{
+    const double key = t.key[line];
+    if (!in_window(w, key))
+        return false;
+    const int ax = t.axis[line];
+    const float second = (ax == 3) ? pos3[1] : pos3[2];
+    const double lproj2 = t.second[line];
+    if (!second_close(second, lproj2, hh, t.box))
+        return false;
+    const double dr2 = calc_dr2(__dsub_rn((double)first, key), __dsub_rn((double)second, lproj2),
+                                t.box);
+    if (dr2 <= (double)__fmul_rn(hh, hh)) {
+        *dr2_out = dr2;
+        return true;
+    }
+    return false;
+}
+
+// Coordinates of the particle in an axis group: (table first, cell second).
+__device__ __forceinline__ void group_coords(int g, const float *pos3, float *first, float *second)
+{
+    if (g == 0) {          // axis 1: keyed by y, filtered on z
+        *first = pos3[1];
+        *second = pos3[2];
+    } else if (g == 1) {   // axis 2: keyed by x, filtered on z
+        *first = pos3[0];
+        *second = pos3[2];
+    } else {               // axis 3: keyed by x, filtered on y
+        *first = pos3[0];
+        *second = pos3[1];
+    }
+}
+
+// Cell range [c0, c0+cn) (mod nc) covering coordinate c +- reach.
+__device__ __forceinline__ void cell_range(double c, double reach, const LineGroup &G, int *c0,
+                                           int *cn)
+{
+    double lo = floor((c - reach) * G.inv_cw);
+    double hi = floor((c + reach) * G.inv_cw);
+    double n = hi - lo + 1.0;
+    if (!(n < (double)G.nc)) {
+        *c0 = 0;
+        *cn = G.nc;
+        return;
+    }
+    long long l = (long long)lo % G.nc;
+    if (l < 0)
+        l += G.nc;
+    *c0 = (int)l;
+    *cn = (int)n;
+}
+
+__device__ __forceinline__ bool in_box(float c, double box)
+{
+    return c >= 0.0f && (double)c <= box;
+}
+
+template <class Visit>
+__device__ __forceinline__ void for_each_pair(const LineTables &t, const float *pos3, float hh,
+                                              Visit &&visit)
+{
+    if (isnan(hh))
+        return;   // dr2 <= NaN is never true
+    Window wmain, wxx;
+    if (t.n_main)
+        wmain = make_window(pos3[0], hh, t.box);
+    if (t.n_xx)
+        wxx = make_window(pos3[1], hh, t.box);
+    if (!(hh > 0.0f) || isinf(hh)) {
+        // hh <= 0 with every coordinate inside [0, box]: the first-coordinate
+        // window is empty (hh == 0) or second_close needs ffm < lproj2 < ffp with
+        // ffm > ffp (hh < 0), so no sightline is accepted.  hh = -inf empties the
+        // window.  Anything else (coordinates outside the box, hh = +inf) tests
+        // every sightline with the exact predicate.
+        if (hh == -INFINITY)
+            return;
+        if (hh <= 0.0f && in_box(pos3[0], t.box) && in_box(pos3[1], t.box) &&
+            in_box(pos3[2], t.box))
+            return;
+        for (int l = 0; l < t.nlos; l++) {
+            const bool xx = (t.axis[l] == 1);
+            double dr2;
+            if (accept(t, l, xx ? wxx : wmain, xx ? pos3[1] : pos3[0], pos3, hh, &dr2))
+                visit(l, dr2);
+        }
+        return;
+    }
+    // Safety margin: relative 1e-6 of hh plus 1e-6 of a cell covers every
+    // rounding in the accept test and in the cell assignment of the lines.
+    const double reach = (double)hh * (1.0 + 1e-6);
+#pragma unroll 1
+    for (int g = 0; g < 3; g++) {
+        const LineGroup &G = t.g[g];
+        if (G.nlines == 0)
+            continue;
+        float f, s;
+        group_coords(g, pos3, &f, &s);
+        if (!isfinite(f) || !isfinite(s))
+            continue;   // with finite hh, a non-finite coordinate never passes dr2 <= hh^2
+        const double r = reach + 1e-6 * G.cw;
+        int a0, an, b0, bn;
+        cell_range((double)f, r, G, &a0, &an);
+        cell_range((double)s, r, G, &b0, &bn);
+        const Window &w = (g == 0) ? wxx : wmain;
+        for (int ia = 0; ia < an; ia++) {
+            int ca = a0 + ia;
+            if (ca >= G.nc)
+                ca -= G.nc;
+            for (int ib = 0; ib < bn; ib++) {
+                int cb = b0 + ib;
+                if (cb >= G.nc)
+                    cb -= G.nc;
+                const int cell = ca * G.nc + cb;
+                const int e1 = G.cell_start[cell + 1];
+                for (int e = G.cell_start[cell]; e < e1; e++) {
+                    const int l = G.cell_line[e];
+                    double dr2;
+                    if (accept(t, l, w, f, pos3, hh, &dr2))
+                        visit(l, dr2);
+                }
+            }
+        }
+    }
+}
+
+__global__ void count_pairs_kernel(LineTables t, Particles p, unsigned long long *line_count,
+                                   unsigned char *part_flag)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+        float pos3[3] = {p.pos[3 * i], p.pos[3 * i + 1], p.pos[3 * i + 2]};
+        const float hh = p.hh[i];
+        int found = 0;
+        for_each_pair(t, pos3, hh, [&](int l, double) {
+            atomicAdd(&line_count[l], 1ull);
+            found = 1;
+        });
+        if (part_flag)
+            part_flag[i] = (unsigned char)found;
+    }
+}
+
+__global__ void emit_pairs_kernel(LineTables t, Particles p, const long long *off,
+                                  unsigned long long *cursor, int *part, double *dr2,
+                                  unsigned *dev_err)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+        float pos3[3] = {p.pos[3 * i], p.pos[3 * i + 1], p.pos[3 * i + 2]};
+        const float hh = p.hh[i];
+        for_each_pair(t, pos3, hh, [&](int l, double d) {
+            const long long slot = off[l] + (long long)atomicAdd(&cursor[l], 1ull);
+            if (slot < off[l + 1]) {
+                part[slot] = (int)i;
+                dr2[slot] = d;
+            } else {
+                atomicOr(dev_err, (unsigned)DEVERR_PAIR_SLOT);
+            }
+        });
+    }
+}
+
+int search_grid(long long n)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long want = (n + 255) / 256;
+    long long cap = (long long)sms * 8;
+    if (want > cap)
+        want = cap;
+    return (int)(want > 0 ? want : 1);
+}
+
+}  // namespace
+
+void launch_count_pairs(const LineTables &t, const Particles &p, unsigned long long *line_count,
+                        unsigned char *part_flag, cudaStream_t s)
+{
+    if (p.n == 0)
+        return;
+    count_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, line_count, part_flag);
+}
+
+void launch_emit_pairs(const LineTables &t, const Particles &p, const long long *off,
+                       unsigned long long *cursor, int *part, double *dr2, unsigned *dev_err,
+                       cudaStream_t s)
+{
+    if (p.n == 0)
+        return;
+    emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, off, cursor, part, dr2, dev_err);
+}
+
+}  // namespace fsg

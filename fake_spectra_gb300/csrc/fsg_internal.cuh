@@ -1,0 +1,112 @@
+// Internal declarations shared by the CUDA translation units of libfsg.
+//
+// Data layout in HBM (one call):
+//   particles   pos[3N] f32, vel[3N] f32, dens[N] f32, temp[N] f32, hh[N] f32
+//               (the caller's arrays, structure-of-arrays except pos/vel)
+//   sightlines  key[L] f64, second[L] f64, axis[L] i32  + one cell grid per axis
+//   pairs       CSR by sightline: off[L+1] i64, part[P] i32, dr2[P] f64
+//   spectra     out[L * nbins] f64 (row per sightline); per-sightline
+//               128-bit fixed-point accumulators live in shared memory
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fsg {
+
+// kernel ids, fake_spectra/singleabs.h:9-12
+enum KernelId { TOP_HAT = 0, SPH_CUBIC = 1, VORONOI = 2, SPH_QUINTIC = 3 };
+
+// Device error bits (written by kernels, read by the host after a call)
+enum DeviceError : unsigned {
+    DEVERR_FIXED_OVERFLOW = 1u,   // a contribution exceeded its sightline's fixed-point range
+    DEVERR_PAIR_SLOT = 2u,        // emit pass found more pairs than the count pass
+    DEVERR_WINDOW_LIMIT = 4u,     // a pixel window or sub-sample count beyond the limits below
+};
+
+// Limits that turn inputs on which the reference loops for ever (or has
+// undefined behaviour: T = 0, h = inf) into an error instead of a hang.
+constexpr double MAX_SUBSAMPLES = 65536.0;       // tau_kern_outer points per pixel
+constexpr long long MAX_COLDEN_WINDOW = 1ll << 26; // pixels of one colden pair
+
+// One axis group of sightlines (all lines with axis a) on an nc x nc grid of
+// transverse cells of width cw.  Lines sit in cells by their (first, second)
+// transverse coordinates; the table key is the reference's multimap key.
+struct LineGroup {
+    int nlines;
+    int nc;
+    double cw, inv_cw;
+    const int *cell_start;   // nc*nc + 1
+    const int *cell_line;    // global line ids, grouped by cell
+};
+
+struct LineTables {
+    LineGroup g[3];          // axis 1, 2, 3
+    const double *key;       // index_table.cpp:12-14: cofm[3i+1] (axis 1) or cofm[3i] (axes 2, 3)
+    const double *second;    // index_table.cpp:33-39: cofm[3i+1] (axis 3) or cofm[3i+2]
+    const int *axis;         // 1-based
+    int nlos;
+    int n_main;              // lines with axis != 1 (the reference's index_table)
+    int n_xx;                // lines with axis == 1 (the reference's index_table_xx)
+    double box;
+};
+
+struct Particles {
+    const float *pos;        // [3N]
+    const float *vel;        // [3N] (tau only)
+    const float *dens;       // [N]
+    const float *temp;       // [N] (tau only)
+    const float *hh;         // [N]
+    long long n;
+};
+
+// LineAbsorption constants (absorption.cpp:152-161) plus the call geometry.
+struct LineParams {
+    int compute_tau;
+    int nbins;
+    int kernel;
+    double tautail;
+    double sigma_a;          // sqrt(3 pi sigma_T / 8) lambda f
+    double bfac;             // sqrt(2 k_B / (m m_p)) / 1e5
+    double voigt_fac;        // Gamma lambda / (4 pi) / 1e5
+    double velfac;
+    double vbox;             // box * velfac
+    double box;
+};
+
+struct PairLists {
+    const long long *off;    // [L+1]
+    const int *part;         // [P]
+    const double *dr2;       // [P]
+};
+
+// Host launchers (stream-ordered; no synchronisation inside).
+void launch_count_pairs(const LineTables &t, const Particles &p, unsigned long long *line_count,
+                        unsigned char *part_flag, cudaStream_t s);
+void launch_emit_pairs(const LineTables &t, const Particles &p, const long long *off,
+                       unsigned long long *cursor, int *part, double *dr2, unsigned *dev_err,
+                       cudaStream_t s);
+
+struct DepositLaunch {
+    int precision;           // 0 = FP64 plain, 1 = FP32 tuned
+    int threads;             // CTA size
+    int persistent;          // 1: grid of resident CTAs draining a ticket queue
+    int grid;                // persistent grid size (CTAs)
+    int smem_mode;           // 1: per-sightline shared-memory accumulators
+};
+
+// Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
+// whose contributions are not all finite are appended to bad_lines (counter
+// *n_bad) and left for deposit_fallback.
+void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
+                    const PairLists &pl, const int *line_order, int nlos, double *out,
+                    unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
+                    unsigned long long *gacc, const DepositLaunch &cfg, cudaStream_t s);
+// Plain FP64 atomics into out for the listed lines (non-finite propagation).
+void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Particles &p,
+                             const PairLists &pl, const int *bad_lines, int n_bad, double *out,
+                             unsigned *dev_err, cudaStream_t s);
+
+int deposit_max_smem_bins();
+
+}  // namespace fsg

@@ -1,0 +1,99 @@
+"""Device-resident entry points (particle arrays already in HBM as torch tensors).
+
+These are what a batched caller uses: the particle arrays live on the GPU,
+the sightline tables (axis, cofm) are small host arrays, and outputs are
+float64 device tensors.  Kernels run on torch's current CUDA stream.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _dptr(t, dtype_name, name):
+    import torch
+    want = {"float32": torch.float32, "float64": torch.float64}[dtype_name]
+    if not t.is_cuda:
+        raise ValueError("%s must be a CUDA tensor" % name)
+    if t.dtype != want:
+        raise TypeError("%s must be %s" % (name, dtype_name))
+    if not t.is_contiguous():
+        raise ValueError("%s must be contiguous" % name)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _host_tables(axis, cofm):
+    axis = np.ascontiguousarray(np.asarray(axis), dtype=None)
+    cofm = np.ascontiguousarray(np.asarray(cofm), dtype=None)
+    if axis.dtype != np.int32:
+        raise TypeError("Axis must be a 32-bit integer\n")
+    if cofm.dtype != np.float64:
+        raise TypeError("Sightline positions must have 64-bit float type\n")
+    if cofm.ndim != 2 or cofm.shape[1] != 3 or cofm.shape[0] != axis.shape[0]:
+        raise ValueError("cofm must have dimensions (np.size(axis),3) \n")
+    return axis, cofm
+
+
+def _bind_stream(ctx):
+    import torch
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+
+
+def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, atime, lam, gamma,
+                                fosc, amumass, tautail, pos, vel, dens, temp, h, axis, cofm,
+                                out=None, precision="fp64", threads=0, persistent=-1):
+    """`_Particle_Interpolate` on device tensors; returns `out` (nlos, nbins) float64 on device."""
+    import torch
+    axis, cofm = _host_tables(axis, cofm)
+    nlos = int(axis.shape[0])
+    npart = int(pos.shape[0])
+    if out is None:
+        out = torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device)
+    args_p = [_dptr(pos, "float32", "pos"),
+              _dptr(vel, "float32", "vel") if compute_tau else None,
+              _dptr(dens, "float32", "dens"),
+              _dptr(temp, "float32", "temp") if compute_tau else None,
+              _dptr(h, "float32", "h")]
+    _bind_stream(ctx)
+    opt = _lib.make_options(precision, threads, persistent)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_particle_interpolate_device(
+        ctx.handle, int(compute_tau), int(nbins), int(kernel), float(box), float(velfac),
+        float(atime), float(lam), float(gamma), float(fosc), float(amumass), float(tautail),
+        *args_p, npart, axis.ctypes.data_as(ctypes.c_void_p),
+        cofm.ctypes.data_as(ctypes.c_void_p), nlos, _dptr(out, "float64", "out"),
+        ctypes.byref(opt), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return out
+
+
+def build_pairs(ctx, box, pos, h, axis, cofm):
+    """Sightline-particle search on the device; returns the number of pairs."""
+    axis, cofm = _host_tables(axis, cofm)
+    _bind_stream(ctx)
+    n = ctypes.c_int64(0)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_build_pairs_device(ctx.handle, float(box), _dptr(pos, "float32", "pos"),
+                                  _dptr(h, "float32", "h"), int(pos.shape[0]),
+                                  axis.ctypes.data_as(ctypes.c_void_p),
+                                  cofm.ctypes.data_as(ctypes.c_void_p), int(axis.shape[0]),
+                                  ctypes.byref(n), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return int(n.value)
+
+
+def copy_pairs(ctx, nlos, npairs, sorted=True):
+    """Pair lists of the last search as CSR numpy arrays (offsets, part, dr2)."""
+    off = np.zeros(nlos + 1, dtype=np.int64)
+    part = np.zeros(max(npairs, 1), dtype=np.int32)
+    dr2 = np.zeros(max(npairs, 1), dtype=np.float64)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_copy_pairs(ctx.handle, off.ctypes.data_as(ctypes.c_void_p),
+                          part.ctypes.data_as(ctypes.c_void_p),
+                          dr2.ctypes.data_as(ctypes.c_void_p), int(bool(sorted)), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return off, part[:npairs], dr2[:npairs]

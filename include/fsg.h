@@ -1,0 +1,122 @@
+/*
+ * fsg.h -- C ABI of libfsg, the GB300 (sm_103a) implementation of
+ * fake_spectra's sightline-interpolation path (`_Particle_Interpolate`).
+ *
+ * Plain C types only: pointers, sizes, doubles.  Every entry returns an
+ * fsg_status; on failure a message is written to errbuf (if non-NULL).
+ * Host-pointer entries behave like the reference call (synchronous, the
+ * output is allocated by the caller and fully written).  Device-pointer
+ * entries take CUDA device pointers for particle arrays and outputs, host
+ * pointers for the (small) sightline tables, and run on the context's
+ * stream; they return after the work has completed.
+ */
+#ifndef FSG_H
+#define FSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The Python layer maps them onto the exception classes the
+ * reference raises (py_module.cpp:117-233). */
+typedef enum {
+    FSG_OK = 0,
+    FSG_ERR_VALUE = 1,           /* bad size/shape/value      -> ValueError     */
+    FSG_ERR_TYPE = 2,            /* wrong element type        -> TypeError      */
+    FSG_ERR_MEMORY = 3,          /* allocation failed         -> MemoryError    */
+    FSG_ERR_CUDA = 4,            /* CUDA runtime failure      -> RuntimeError   */
+    FSG_ERR_NOT_IMPLEMENTED = 5, /* Voronoi kernel (kernel==2) -> NotImplementedError */
+    FSG_ERR_DEVICE = 6           /* a kernel reported an internal limit        */
+} fsg_status;
+
+/* Arithmetic form of the deposit. */
+typedef enum {
+    FSG_PREC_FP64 = 0, /* plain form: FP64 everywhere (the drop-in default) */
+    FSG_PREC_FP32 = 1  /* tuned form: FP32 profile/kernel arithmetic        */
+} fsg_precision;
+
+typedef struct {
+    int precision;  /* fsg_precision                                         */
+    int threads;    /* threads per deposit CTA; 0 = default/autotuned        */
+    int persistent; /* -1 = default, 0 = one CTA per sightline, 1 = resident
+                       CTAs draining a sightline queue                        */
+    int reserved[5];
+} fsg_options;
+
+typedef struct {
+    int64_t npairs;          /* sightline-particle pairs of the last search    */
+    int64_t gpu_launches;    /* kernels this context has launched (cumulative) */
+    int32_t fallback_lines;  /* sightlines re-run for non-finite contributions */
+    int32_t reserved;
+    double ms_search;        /* device time of the last pair search            */
+    double ms_deposit;       /* device time of the last deposit                */
+} fsg_stats;
+
+typedef struct fsg_context fsg_context;
+
+/* Library version string. */
+const char *fsg_version(void);
+
+/* Context: one device, one stream, a grow-only device workspace and the pair
+ * lists of the last search. */
+int fsg_context_create(int device, fsg_context **ctx, char *errbuf, size_t errlen);
+void fsg_context_destroy(fsg_context *ctx);
+/* Use a caller-owned cudaStream_t (NULL = the context's own stream). */
+int fsg_context_set_stream(fsg_context *ctx, void *cuda_stream);
+int fsg_context_stats(const fsg_context *ctx, fsg_stats *out);
+
+/*
+ * Drop-in for _spectra_priv._Particle_Interpolate
+ * (fake_spectra/py_module.cpp:103-233, Py_Particle_Interpolation), with the
+ * same positional arguments and units:
+ *   compute_tau  1: optical depth (ParticleInterp::compute_tau, part_int.cpp:20-51)
+ *                0: column density (ParticleInterp::compute_colden, part_int.cpp:53-84)
+ *   pos, vel     [npart*3] float32; vel and temp are not read when compute_tau == 0
+ *   dens, temp, h [npart] float32
+ *   axis [nlos] int32 (1, 2 or 3), cofm [nlos*3] float64
+ *   out  [nlos*nbins] float64, written completely (zero where nothing absorbs)
+ * All pointers are HOST pointers.  opt may be NULL (plain FP64 form).
+ * Uses a library-owned context for device 0 (or the current device).
+ */
+int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box, double velfac,
+                             double atime, double lambda, double gamma, double fosc,
+                             double amumass, double tautail, const float *pos, const float *vel,
+                             const float *dens, const float *temp, const float *h, int64_t npart,
+                             const int32_t *axis, const double *cofm, int32_t nlos, double *out,
+                             const fsg_options *opt, char *errbuf, size_t errlen);
+
+/* Same computation with DEVICE pointers for pos/vel/dens/temp/h/out; axis and
+ * cofm stay HOST pointers. */
+int fsg_particle_interpolate_device(fsg_context *ctx, int compute_tau, int nbins, int kernel,
+                                    double box, double velfac, double atime, double lambda,
+                                    double gamma, double fosc, double amumass, double tautail,
+                                    const float *pos, const float *vel, const float *dens,
+                                    const float *temp, const float *h, int64_t npart,
+                                    const int32_t *axis, const double *cofm, int32_t nlos,
+                                    double *out, const fsg_options *opt, char *errbuf,
+                                    size_t errlen);
+
+/*
+ * Sightline-particle search alone: replaces IndexTable::get_near_particles
+ * (fake_spectra/index_table.cpp:130-150).  pos/h are DEVICE pointers; axis/cofm
+ * HOST.  The pair lists stay in the context; *npairs receives their total.
+ */
+int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const float *h,
+                           int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
+                           int64_t *npairs, char *errbuf, size_t errlen);
+
+/* Copy the context's pair lists to HOST buffers as CSR by sightline:
+ * offsets[nlos+1], part[npairs], dr2[npairs].  Within a sightline the pairs
+ * are sorted by ascending particle index (the std::map order of the
+ * reference) when sorted != 0, else in arrival order. */
+int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr2, int sorted,
+                   char *errbuf, size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSG_H */
