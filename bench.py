@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark of the sightline-interpolation path (`_Particle_Interpolate`) on GB300.
+
+One step = one full call for the Ly-a line over every sightline of the
+workload: the sightline-particle search and the tau deposit, inputs resident
+in HBM (device API).  `value` is Ly-a tau pixels/s of the tuned FP32 form
+(sightlines x pixels per call / call time), whole job over all ranks.
+
+Beside it, on the same workload:
+  fp64_plain   the plain FP64 form (on a stated sightline subset when the full
+               set would take minutes: FP64 runs at 1/64 of the FP32 rate here);
+  accuracy     max|dF|, relative tau error and column-density error of the FP32
+               form against the FP64 form on those sightlines;
+  e2e          the same metric through the host-pointer C ABI call
+               (fsg_particle_interpolate), with the host<->device copies timed;
+  roofline     the deposit kernel against the FP32 FMA-pipe peak measured by
+               the library's own microbenchmark, from exact work counts;
+  cpu_baseline the CPU oracle (C restatement of the reference, OpenMP, all
+               host cores) on a stated sample of sightlines.
+
+`--impl reference` times the CPU implementation alone (the oracle; the
+reference sources are not on the GPU machine) on the same workload.
+Multi-GPU: independent replicas (the path is not sharded), weak scaling.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BASELINE_METRIC = ("Ly-α tau pixels/s, tuned FP32 vs plain FP64 GPU at max|ΔF|≤1e-4; "
+                   "fwd+bwd ms")
+
+# Algorithmic flops per Voigt-profile evaluation, counted once from the source
+# of each branch (fsg_voigt.cuh) plus the 3-4 flops of the node sum in
+# tau_kern_inner; FMA = 2 flops, MUFU ops = 1.
+FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214}
+FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="fsg", choices=["fsg", "reference"])
+    p.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4])
+    p.add_argument("--nside", type=int, default=0, help="particles per side (0 = the config's)")
+    p.add_argument("--nlos", type=int, default=0, help="sightlines (0 = the config's)")
+    p.add_argument("--fp64-lines", type=int, default=512,
+                   help="sightlines timed in the plain FP64 form (0 = all)")
+    p.add_argument("--cpu-lines", type=int, default=16,
+                   help="sightlines in the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def make_workload(args, device):
+    from fake_spectra_gb300 import synth
+    return synth.generate_torch(args.config, device=device, nside=args.nside or None,
+                                nlos=args.nlos or None)
+
+
+def subset_lines(nlos, k, seed=12345):
+    if k <= 0 or k >= nlos:
+        return np.arange(nlos)
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(nlos, size=k, replace=False))
+
+
+def cpu_sample(w_host, lines, threads):
+    """Time the CPU oracle on a subset of sightlines; returns (pixels/s, seconds)."""
+    import oracle
+    port = oracle.port()
+    port.set_threads(threads)
+    from fake_spectra_gb300 import synth
+    args = list(w_host.call_args(synth.LYA, 1))
+    args[16] = w_host.axis[lines]
+    args[17] = w_host.cofm[lines]
+    t0 = time.perf_counter()
+    port.particle_interpolate(*args)
+    dt = time.perf_counter() - t0
+    return len(lines) * w_host.nbins / dt, dt
+
+
+def run_reference(args):
+    rank, world, local = dist_setup()
+    if rank != 0:
+        return
+    import torch
+    from fake_spectra_gb300 import synth  # noqa: F401
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    w = make_workload(args, dev).to_host()
+    threads = os.cpu_count() or 1
+    lines = subset_lines(w.nlos, args.cpu_lines)
+    for _ in range(args.warmup):
+        cpu_sample(w, lines[:max(1, len(lines) // 4)], threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        v, s = cpu_sample(w, lines, threads)
+        vals.append(v)
+        secs.append(s)
+    value = len(lines) * w.nbins * len(secs) / sum(secs)
+    sample = ("CPU oracle (C restatement of the reference path, OpenMP) on %d of %d sightlines "
+              "with all %d particles, per step" % (len(lines), w.nlos, w.npart))
+    print(json.dumps({
+        "impl": "reference", "metric": BASELINE_METRIC, "value": value, "unit": "pixels/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "particles": w.npart, "sightlines": w.nlos,
+                   "nbins": w.nbins, "line": "Ly-a 1215.67 A", "kernel": "cubic spline"},
+        "cpu_baseline": {"value": value, "unit": "pixels/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pixels/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    from fake_spectra_gb300 import build, synth, interp, _lib
+    build.build()
+    w = make_workload(args, "cuda")
+    torch.cuda.synchronize()
+    ctx = _lib.Context(local)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    lya = synth.LYA
+    targs = w.call_args(lya, 1)
+    pixels = w.nlos * w.nbins
+    out = torch.empty((w.nlos, w.nbins), dtype=torch.float64, device="cuda")
+
+    def step(precision, o=out, lines=None, count=False):
+        a = list(targs)
+        if lines is not None:
+            a[16] = w.axis[lines]
+            a[17] = w.cofm[lines]
+        return interp.particle_interpolate_device(ctx, *a, out=o, precision=precision,
+                                                  count_work=count)
+
+    # ---- tuned FP32 form: the timed region
+    for _ in range(args.warmup):
+        step("fp32")
+    stream = torch.cuda.current_stream()
+    launches0 = ctx.stats()["gpu_launches"]
+    clocks = ClockSampler(local).start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    dep_ms, search_ms = [], []
+    for _ in range(args.steps):
+        step("fp32")
+        st = ctx.stats()
+        dep_ms.append(st["ms_deposit"])
+        search_ms.append(st["ms_search"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    launches = ctx.stats()["gpu_launches"] - launches0
+    ms_step = allreduce_max(ev0.elapsed_time(ev1) / args.steps, world)
+    value = world * pixels / (ms_step * 1e-3)
+    tau32 = out.clone()
+    npairs = ctx.stats()["npairs"]
+
+    # ---- work counts for the roofline (untimed counting variant)
+    step("fp32", o=torch.empty_like(out), count=True)
+    cnt = ctx.stats()
+    flops = sum(cnt["evals_" + k] * FLOPS_FP32[k] for k in ("core", "wing", "other"))
+    dep_mean = sum(dep_ms) / len(dep_ms)
+    peak32 = _lib.fma_peak_tflops("fp32")
+    achieved = flops / (dep_mean * 1e-3) / 1e12
+    res = {
+        "metric": BASELINE_METRIC, "value": value, "unit": "pixels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded torch generator following the BASELINE config recipe",
+        "config": {"workload": w.name, "particles": w.npart, "sightlines": w.nlos,
+                   "nbins": w.nbins, "pairs": npairs, "line": "Ly-a 1215.67 A",
+                   "kernel": "cubic spline", "form": "FP32 tuned (persistent sightline queue)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (%.2f GB of particle arrays)" % (w.npart * 36 / 1e9)},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "phases_ms": {"search": sum(search_ms) / len(search_ms), "deposit": dep_mean},
+        "roofline": {"bound": "fp32-pipe", "kernel": "deposit_kernel<tau, FP32>",
+                     "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                     "frac": achieved / peak32,
+                     "peak_source": "measured: libfsg FMA-chain microbenchmark (MEASURED_PEAKS.json "
+                                    "has no FP32 figure)",
+                     "work": {"evals_core": cnt["evals_core"], "evals_wing": cnt["evals_wing"],
+                              "evals_other": cnt["evals_other"], "pixels": cnt["pixels"],
+                              "flops_per_eval": FLOPS_FP32},
+                     "traffic": None},
+    }
+
+    # ---- plain FP64 form on a sightline subset, and the accuracy of FP32 against it
+    if not args.no_fp64:
+        lines = subset_lines(w.nlos, args.fp64_lines)
+        o64 = torch.empty((len(lines), w.nbins), dtype=torch.float64, device="cuda")
+        step("fp64", o=o64, lines=lines)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step("fp64", o=o64, lines=lines)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        v64 = len(lines) * w.nbins / (ms64 * 1e-3)
+        # FP32 on the same subset (same call shape) for a like-for-like ratio
+        o32 = torch.empty_like(o64)
+        step("fp32", o=o32, lines=lines)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        step("fp32", o=o32, lines=lines)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32s = e0.elapsed_time(e1)
+        t64 = o64.cpu().numpy()
+        t32 = tau32[torch.from_numpy(lines).cuda()].cpu().numpy()
+        dF = np.abs(np.exp(-t32) - np.exp(-t64))
+        big = t64 >= 1e-3
+        rel = np.abs(t32 - t64)[big] / t64[big] if big.any() else np.zeros(1)
+        # column density, both forms
+        cargs = list(w.call_args(lya, 0))
+        cargs[16], cargs[17] = w.axis[lines], w.cofm[lines]
+        c64 = interp.particle_interpolate_device(ctx, *cargs, precision="fp64").cpu().numpy()
+        c32 = interp.particle_interpolate_device(ctx, *cargs, precision="fp32").cpu().numpy()
+        nz = c64 != 0
+        crel = np.abs(c32 - c64)[nz] / np.abs(c64[nz]) if nz.any() else np.zeros(1)
+        res["fp64_plain"] = {"value": v64, "unit": "pixels/s", "ms_per_call": ms64,
+                             "sightlines": int(len(lines)),
+                             "fp32_same_subset": {"value": len(lines) * w.nbins / (ms32s * 1e-3),
+                                                  "ms_per_call": ms32s},
+                             "fp32_over_fp64": (len(lines) * w.nbins / (ms32s * 1e-3)) / v64}
+        res["accuracy"] = {"max_abs_dF": float(dF.max()), "tau_rel_err_max": float(rel.max()),
+                           "tau_rel_err_median": float(np.median(rel)),
+                           "colden_rel_err_max": float(crel.max()),
+                           "against": "plain FP64 form on the same %d sightlines" % len(lines)}
+
+    # ---- end to end through the host-pointer C ABI (copies inside the timed region)
+    if not args.no_e2e:
+        from fake_spectra_gb300._spectra_priv import _Particle_Interpolate
+        pin = lambda t: t.cpu().pin_memory().numpy()
+        h = [pin(x) for x in (w.pos, w.vel, w.dens["HI"], w.temp, w.hh)]
+        hargs = list(targs[:11]) + h + [w.axis, w.cofm]
+        _Particle_Interpolate(*hargs, precision="fp32")
+        ke = max(1, min(args.steps, 3))
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            tau_h = _Particle_Interpolate(*hargs, precision="fp32")
+        dt = allreduce_max((time.perf_counter() - t0) / ke, world)
+        res["e2e"] = {"value": world * pixels / dt, "unit": "pixels/s",
+                      "h2d_bytes_per_step": int(sum(x.nbytes for x in h)),
+                      "d2h_bytes_per_step": int(tau_h.nbytes),
+                      "ms_per_step": dt * 1e3, "api": "fsg_particle_interpolate (host pointers)"}
+
+    # ---- CPU baseline: the oracle on a bounded sample of the same workload
+    if not args.no_cpu and rank == 0 and world == 1:
+        wh = w.to_host()
+        threads = os.cpu_count() or 1
+        lines = subset_lines(w.nlos, args.cpu_lines, seed=777)
+        v, s = cpu_sample(wh, lines, threads)
+        res["cpu_baseline"] = {"value": v, "unit": "pixels/s", "cores": threads, "kind": "port",
+                               "sample": "CPU oracle (C restatement, OpenMP) on %d random of %d "
+                                         "sightlines with all %d particles: %.1f s"
+                                         % (len(lines), w.nlos, w.npart, s)}
+    if rank == 0:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

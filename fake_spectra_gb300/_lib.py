@@ -24,6 +24,7 @@ FSG_PREC_FP32 = 1
 # Names exported by libfsg.so, one per declaration in include/fsg.h.
 EXPORTS = (
     "fsg_version",
+    "fsg_measure_fma_peak",
     "fsg_context_create",
     "fsg_context_destroy",
     "fsg_context_set_stream",
@@ -44,12 +45,14 @@ _c_size = ctypes.c_size_t
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", _c_int), ("threads", _c_int), ("persistent", _c_int),
-                ("reserved", _c_int * 5)]
+                ("count_work", _c_int), ("reserved", _c_int * 4)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("npairs", _c_i64), ("gpu_launches", _c_i64), ("fallback_lines", _c_i32),
-                ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d)]
+                ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d),
+                ("evals_core", _c_i64), ("evals_wing", _c_i64), ("evals_other", _c_i64),
+                ("pixels", _c_i64)]
 
 
 class FsgError(RuntimeError):
@@ -97,6 +100,7 @@ def load(path=None):
                               "fake_spectra_gb300.build.build() on a machine with nvcc" % path)
         L = ctypes.CDLL(path)
         L.fsg_version.restype = ctypes.c_char_p
+        L.fsg_measure_fma_peak.argtypes = [_c_int, ctypes.POINTER(_c_d), _p, _c_size]
         L.fsg_context_create.argtypes = [_c_int, ctypes.POINTER(_p), _p, _c_size]
         L.fsg_context_destroy.argtypes = [_p]
         L.fsg_context_destroy.restype = None
@@ -115,8 +119,9 @@ def errbuf():
     return ctypes.create_string_buffer(512)
 
 
-def make_options(precision="fp64", threads=0, persistent=-1):
+def make_options(precision="fp64", threads=0, persistent=-1, count_work=False):
     o = Options()
+    o.count_work = int(bool(count_work))
     if precision in ("fp64", FSG_PREC_FP64):
         o.precision = FSG_PREC_FP64
     elif precision in ("fp32", FSG_PREC_FP32):
@@ -152,7 +157,9 @@ class Context:
         self._lib.fsg_context_stats(self._h, ctypes.byref(s))
         return {"npairs": int(s.npairs), "gpu_launches": int(s.gpu_launches),
                 "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
-                "ms_deposit": float(s.ms_deposit)}
+                "ms_deposit": float(s.ms_deposit), "evals_core": int(s.evals_core),
+                "evals_wing": int(s.evals_wing), "evals_other": int(s.evals_other),
+                "pixels": int(s.pixels)}
 
     def close(self):
         if self._h:
@@ -164,3 +171,13 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def fma_peak_tflops(precision="fp32"):
+    """Peak FMA throughput of the current GPU (TFLOP/s), own microbenchmark."""
+    L = load()
+    v = _c_d(0.0)
+    eb = errbuf()
+    prec = FSG_PREC_FP64 if precision in ("fp64", FSG_PREC_FP64) else FSG_PREC_FP32
+    raise_for(L.fsg_measure_fma_peak(prec, ctypes.byref(v), eb, 512), eb.value.decode())
+    return float(v.value)

@@ -74,7 +74,7 @@ struct fsg_context {
     DevBuf pos, vel, dens, temp, hh, out;                    // staging for host-pointer calls
     DevBuf key, second, axis, cell_start[3], cell_line[3];   // sightline tables
     DevBuf line_count, cursor, off, part, dr2, line_order;   // pair lists
-    DevBuf ticket, bad, nbad, err, gacc;                     // deposit bookkeeping
+    DevBuf ticket, bad, nbad, err, gacc, counters;           // deposit bookkeeping
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // host mirrors
     std::vector<long long> h_off;
@@ -105,7 +105,7 @@ struct fsg_context {
         DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis,
                           &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
                           &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
-                          &line_order, &ticket, &bad, &nbad, &err, &gacc};
+                          &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -286,15 +286,29 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
     DepositLaunch cfg{};
     cfg.precision = opt ? opt->precision : FSG_PREC_FP64;
-    cfg.threads = (opt && opt->threads > 0) ? opt->threads : 256;
+    if (cfg.precision != FSG_PREC_FP64 && cfg.precision != FSG_PREC_FP32)
+        fail(FSG_ERR_VALUE, "unknown precision %d", cfg.precision);
+    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
+    cfg.threads = (opt && opt->threads > 0) ? opt->threads : tmax;
+    if (cfg.threads % 32 || cfg.threads > tmax)
+        fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
     cfg.smem_mode = lp.nbins <= deposit_max_smem_bins();
-    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent : 0;
+    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent
+                                                    : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    cfg.grid = std::min(nlos, sms * 2);
+    const int per_sm = std::max(1, deposit_resident_ctas(lp.compute_tau, cfg.precision,
+                                                         cfg.threads, lp.nbins, cfg.smem_mode));
+    cfg.grid = std::min(nlos, sms * per_sm);
     unsigned long long *gacc = nullptr;
     if (!cfg.smem_mode) {
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
+    }
+    const bool count = opt && opt->count_work;
+    unsigned long long *ctr = nullptr;
+    if (count) {
+        ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 4);
+        cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 4, s), "memset");
     }
     auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
     auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
@@ -304,7 +318,7 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int), s), "memset");
     cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
     launch_deposit(lp, c->tables, p, pl, (const int *)c->line_order.p, nlos, out, ticket, bad,
-                   nbad, err, gacc, cfg, s);
+                   nbad, err, gacc, ctr, cfg, s);
     c->stats.gpu_launches++;
     cuda_check(cudaGetLastError(), "deposit launch");
     int h_nbad = 0;
@@ -324,6 +338,14 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
     c->stats.ms_deposit = ms;
+    if (count) {
+        unsigned long long h_ctr[4];
+        cuda_check(cudaMemcpy(h_ctr, ctr, sizeof h_ctr, cudaMemcpyDeviceToHost), "read counters");
+        c->stats.evals_core = (int64_t)h_ctr[0];
+        c->stats.evals_wing = (int64_t)h_ctr[1];
+        c->stats.evals_other = (int64_t)h_ctr[2];
+        c->stats.pixels = (int64_t)h_ctr[3];
+    }
     if (h_err)
         fail(FSG_ERR_DEVICE, "deposit kernel reported device error bits 0x%x", h_err);
 }
@@ -380,7 +402,26 @@ void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, dou
 
 extern "C" {
 
-const char *fsg_version(void) { return "fsg 0.1 (sm_103a)"; }
+const char *fsg_version(void) { return "fsg 0.2 (sm_103a)"; }
+
+int fsg_measure_fma_peak(int precision, double *tflops, char *errbuf, size_t errlen)
+{
+    try {
+        if (!tflops)
+            fail(FSG_ERR_VALUE, "tflops is NULL");
+        if (precision != FSG_PREC_FP64 && precision != FSG_PREC_FP32)
+            fail(FSG_ERR_VALUE, "unknown precision %d", precision);
+        const double v = measure_fma_peak(precision, 0);
+        cuda_check(cudaGetLastError(), "fma peak");
+        cuda_check(cudaDeviceSynchronize(), "fma peak");
+        if (!(v > 0))
+            fail(FSG_ERR_CUDA, "fma peak measurement failed");
+        *tflops = v;
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
 
 int fsg_context_create(int device, fsg_context **ctx, char *errbuf, size_t errlen)
 {

@@ -5,74 +5,85 @@
 // (singleabs.h:63-175).
 //
 // Work decomposition: one CTA owns one sightline at a time (sightlines are
-// visited in descending pair count); each warp takes one (particle,
-// sightline) pair at a time and walks its pixel window 32 pixels per step.
+// visited in descending pair count, either one CTA per sightline or resident
+// CTAs draining a ticket queue); each warp takes one (particle, sightline)
+// pair at a time and walks its pixel window 32 pixels per step.
 // tau: forward from zmax and backward from zmax-1, each direction stopping
 // after the first pixel whose contribution is below tautail (that pixel is
 // still added) or after nbins/2 pixels, exactly the rule of
 // absorption.cpp:250-278; the warp finds the stop lane with a ballot.
 // colden: the fixed pixel range of absorption.cpp:190-209.
 //
+// Two arithmetic forms share this skeleton:
+//   FP64 (plain): every quantity in double, as the reference computes it.
+//   FP32 (tuned): profile, kernel and pixel arithmetic in float; double only
+//     for the particle velocity, the bin of the particle (zmax) and the offset
+//     of the first pixel from it, so box-sized coordinates lose nothing.
+//
 // Accumulation: every contribution is converted to a 128-bit two's-complement
 // fixed-point integer with a per-sightline scale 2^S, S chosen from an upper
 // bound of that sightline's total so nothing can overflow, and added with
-// 64-bit integer atomics (low word + carry into the high word).  Integer
-// addition is associative, so the result does not depend on the order in
-// which warps and pairs arrive: the output is bitwise deterministic, and the
-// sum is exact up to the final rounding to double.  Sightlines with a
-// non-finite contribution (inf/NaN inputs) are re-run by a plain FP64-atomic
-// fallback so that inf/NaN propagate as they do in the reference.
+// 64-bit integer atomics (low word + carry into the high word) into
+// per-sightline accumulators in shared memory.  Integer addition is
+// associative, so the result does not depend on the order in which warps and
+// pairs arrive: the output is bitwise deterministic and the sum is exact up to
+// the final rounding to double.  Sightlines with a non-finite contribution
+// (inf/NaN inputs) are re-run by a plain FP64-atomic fallback so that inf/NaN
+// propagate as they do in the reference.
 #include "fsg_internal.cuh"
 #include "fsg_voigt.cuh"
-
-#include <cfloat>
 
 namespace fsg {
 
 namespace {
 
-constexpr int NGRID = 8;                          // singleabs.h:8
+constexpr int NGRID = 8;                           // singleabs.h:8
+constexpr int NODES = NGRID - 1;                   // interior nodes of tau_kern_inner
 constexpr double PI_D = 3.14159265358979323846;
-constexpr double LIGHT_KMS = 2.99792458e10 / 1e5;  // absorption.cpp:26, km/s
+constexpr double LIGHT_KMS = 2.99792458e10 / 1e5;  // absorption.cpp:26, in km/s
 
-// ---------------------------------------------------------------- kernels
-__device__ __forceinline__ double cubic_kernel(double q)   // singleabs.h:17-26
+// ------------------------------------------------------------ SPH kernels
+template <class T>
+__device__ __forceinline__ T cubic_kernel(T q)   // singleabs.h:17-26
 {
-    const double norm = 32. / 4 / PI_D;
-    if (q >= 1)
-        return 0;
-    if (q < 0.5)
-        return norm * (1 - 6 * q * q + 6 * q * q * q);
-    const double t = 1. - q;
-    return norm * (2 * t * t * t);
+    const T norm = (T)(32. / 4 / PI_D);
+    if (q >= (T)1)
+        return (T)0;
+    if (q < (T)0.5)
+        return norm * ((T)1 - (T)6 * q * q + (T)6 * q * q * q);
+    const T t = (T)1 - q;
+    return norm * ((T)2 * t * t * t);
 }
 
-__device__ __forceinline__ double quintic_kernel(double q)  // singleabs.h:31-42
+template <class T>
+__device__ __forceinline__ T quintic_kernel(T q)  // singleabs.h:31-42
 {
-    const double norm = 9. / 40 / PI_D;
-    if (q >= 1)
-        return 0;
-    if (q < (1. / 3))
-        return norm * 6 * (11 - 90 * q * q + 405 * q * q * q * q - 405 * q * q * q * q * q);
-    if (q < (2. / 3)) {
-        const double a = 3. - 3 * q, b = 2. - 3 * q;
-        return norm * (a * a * a * a * a - 6 * b * b * b * b * b);
+    const T norm = (T)(9. / 40 / PI_D);
+    if (q >= (T)1)
+        return (T)0;
+    if (q < (T)(1. / 3))
+        return norm * (T)6 *
+               ((T)11 - (T)90 * q * q + (T)405 * q * q * q * q - (T)405 * q * q * q * q * q);
+    if (q < (T)(2. / 3)) {
+        const T a = (T)3 - (T)3 * q, b = (T)2 - (T)3 * q;
+        return norm * (a * a * a * a * a - (T)6 * b * b * b * b * b);
     }
-    const double t = 1. - q;
-    return norm * (243 * t * t * t * t * t);
+    const T t = (T)1 - q;
+    return norm * ((T)243 * t * t * t * t * t);
 }
 
 // Weight of one line-of-sight node in tau_kern_inner (singleabs.h:158-163):
 // unknown kernel ids get no weight factor.
-__device__ __forceinline__ double node_weight(int kernel, double q)
+template <class T>
+__device__ __forceinline__ T node_weight(int kernel, T q)
 {
     if (kernel == SPH_CUBIC)
-        return cubic_kernel(q);
+        return cubic_kernel<T>(q);
     if (kernel == SPH_QUINTIC)
-        return quintic_kernel(q);
+        return quintic_kernel<T>(q);
     if (kernel == TOP_HAT)
-        return 3. / 4. / PI_D;
-    return 1.0;
+        return (T)(3. / 4. / PI_D);
+    return (T)1;
 }
 
 __device__ __forceinline__ double kernel_max(int kernel)
@@ -87,8 +98,8 @@ __device__ __forceinline__ double kernel_max(int kernel)
 }
 
 // absorption.cpp:53-115: line-of-sight integral of the kernel over one pixel
-__device__ double kern_frac(int kernel, double zlow, double zhigh, double smooth, double dr2,
-                            double zrange)
+template <class T>
+__device__ T kern_frac(int kernel, T zlow, T zhigh, T smooth, T dr2, T zrange)
 {
     if (zlow < -zrange)
         zlow = -zrange;
@@ -96,39 +107,34 @@ __device__ double kern_frac(int kernel, double zlow, double zhigh, double smooth
         zhigh = zrange;
     if (kernel == SPH_CUBIC || kernel == SPH_QUINTIC) {
         if (zlow > zhigh)
-            return 0;
+            return (T)0;
         const bool cub = (kernel == SPH_CUBIC);
-        double q = sqrt(dr2 + zlow * zlow) / smooth;
-        double total = (cub ? cubic_kernel(q) : quintic_kernel(q)) / 2.;
-        const double deltaz = (zhigh - zlow) / NGRID;
+        T q = sqrt(dr2 + zlow * zlow) / smooth;
+        T total = (cub ? cubic_kernel<T>(q) : quintic_kernel<T>(q)) / (T)2;
+        const T deltaz = (zhigh - zlow) / (T)NGRID;
         for (int i = 1; i < NGRID; ++i) {
-            const double zz = i * deltaz + zlow;
+            const T zz = (T)i * deltaz + zlow;
             q = sqrt(dr2 + zz * zz) / smooth;
-            total += cub ? cubic_kernel(q) : quintic_kernel(q);
+            total += cub ? cubic_kernel<T>(q) : quintic_kernel<T>(q);
         }
         q = sqrt(dr2 + zhigh * zhigh) / smooth;
-        total += (cub ? cubic_kernel(q) : quintic_kernel(q)) / 2.;
+        total += (cub ? cubic_kernel<T>(q) : quintic_kernel<T>(q)) / (T)2;
         return deltaz * total;
     }
-    const double d = zhigh - zlow;
-    return 3. / 4. / PI_D * (d > 0. ? d : 0.);
+    const T d = zhigh - zlow;
+    return (T)(3. / 4. / PI_D) * (d > (T)0 ? d : (T)0);
 }
 
 // ------------------------------------------------- 128-bit fixed point
-__device__ __forceinline__ bool to_fixed(double c, int S, unsigned long long &lo,
-                                         unsigned long long &hi)
+// value * 2^S as a 128-bit two's-complement integer (round to nearest).
+// Returns false if it would not fit in 126 bits.
+__device__ __forceinline__ bool mant_to_fixed(unsigned long long m, int sh, bool neg,
+                                              unsigned long long &lo, unsigned long long &hi,
+                                              int mbits)
 {
-    const long long bits = __double_as_longlong(c);
-    unsigned long long m = (unsigned long long)bits & 0xFFFFFFFFFFFFFull;
-    int e = (int)((bits >> 52) & 0x7FF);
-    if (e == 0)
-        e = 1;
-    else
-        m |= (1ull << 52);
-    const int sh = e - 1075 + S;
     unsigned long long l, h;
     if (sh >= 0) {
-        if (sh > 126 - 53)
+        if (sh > 126 - mbits)
             return false;
         if (sh == 0) {
             l = m;
@@ -145,13 +151,39 @@ __device__ __forceinline__ bool to_fixed(double c, int S, unsigned long long &lo
         h = 0;
         l = (r > 63) ? 0ull : ((m + (1ull << (r - 1))) >> r);
     }
-    if (bits < 0) {
+    if (neg) {
         l = ~l + 1ull;
         h = ~h + (l == 0ull ? 1ull : 0ull);
     }
     lo = l;
     hi = h;
     return true;
+}
+
+__device__ __forceinline__ bool to_fixed(double c, int S, unsigned long long &lo,
+                                         unsigned long long &hi)
+{
+    const long long bits = __double_as_longlong(c);
+    unsigned long long m = (unsigned long long)bits & 0xFFFFFFFFFFFFFull;
+    int e = (int)((bits >> 52) & 0x7FF);
+    if (e == 0)
+        e = 1;
+    else
+        m |= (1ull << 52);
+    return mant_to_fixed(m, e - 1075 + S, bits < 0, lo, hi, 53);
+}
+
+__device__ __forceinline__ bool to_fixed(float c, int S, unsigned long long &lo,
+                                         unsigned long long &hi)
+{
+    const int bits = __float_as_int(c);
+    unsigned long long m = (unsigned long long)(bits & 0x7FFFFF);
+    int e = (bits >> 23) & 0xFF;
+    if (e == 0)
+        e = 1;
+    else
+        m |= (1ull << 23);
+    return mant_to_fixed(m, e - 150 + S, bits < 0, lo, hi, 24);
 }
 
 __device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long long *hi, int j,
@@ -180,7 +212,7 @@ __device__ __forceinline__ int wrap_bin(long long z, int nbins)
     return (int)j;
 }
 
-// ------------------------------------------------------ per-pair state
+// ------------------------------------------------------ per-pair inputs
 struct PairInput {
     double dr2;
     float dens, ppos, pvel, temp, smooth;
@@ -193,12 +225,12 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
     const int ip = pl.part[e];
     in.dr2 = pl.dr2[e];
     const long long k = 3ll * ip + axis - 1;
-    in.ppos = p.pos[k];
-    in.dens = p.dens[ip];
-    in.smooth = p.hh[ip];
+    in.ppos = __ldg(&p.pos[k]);
+    in.dens = __ldg(&p.dens[ip]);
+    in.smooth = __ldg(&p.hh[ip]);
     if (tau) {
-        in.pvel = p.vel[k];
-        in.temp = p.temp[ip];
+        in.pvel = __ldg(&p.vel[k]);
+        in.temp = __ldg(&p.temp[ip]);
     } else {
         in.pvel = 0.f;
         in.temp = 0.f;
@@ -206,74 +238,207 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
     return in;
 }
 
-// SingleAbsorber (singleabs.h:81-90) + the per-particle constants of add_tau_particle
-struct TauPair {
-    double btherm, half_b, inv_b, aa, vel, ampd, deltav;
-    double vv[NGRID - 1], w[NGRID - 1];
-    long long zmax;
+// Work counters of the counting variant (per lane, reduced per CTA at exit).
+struct Counters {
+    unsigned long long a, b, c, pixels;
 };
 
-__device__ __forceinline__ bool tau_setup(const LineParams &lp, const PairInput &in, TauPair &s)
-{
-    const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-    if (hh2 - in.dr2 <= 0)
-        return false;   // absorption.cpp:232
-    s.btherm = lp.bfac * sqrt((double)in.temp);
-    s.half_b = s.btherm / 2.;
-    s.inv_b = 1.0 / s.btherm;
-    s.vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
-    const double vdr2 = (lp.velfac * in.dr2) * lp.velfac;
-    const double vsmooth = lp.velfac * (double)in.smooth;
-    s.aa = lp.voigt_fac / s.btherm;
-    const double vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
-    s.deltav = 2. * vhigh / NGRID;
+__device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// ------------------------------------------------ FP64 (plain form) pair
+// SingleAbsorber (singleabs.h:81-90) + the per-particle constants of add_tau_particle
+struct Tau64 {
+    double btherm, half_b, inv_b, aa, vel, ampd, deltav, bintov, velfac;
+    double vv[NODES], w[NODES];
+    long long zmax;
+    int nbins;
+
+    __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
+    {
+        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+        if (hh2 - in.dr2 <= 0)
+            return false;   // absorption.cpp:232
+        btherm = lp.bfac * sqrt((double)in.temp);
+        half_b = btherm / 2.;
+        inv_b = 1.0 / btherm;
+        vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
+        const double vdr2 = (lp.velfac * in.dr2) * lp.velfac;
+        const double vsmooth = lp.velfac * (double)in.smooth;
+        aa = lp.voigt_fac / btherm;
+        const double vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
+        deltav = 2. * vhigh / NGRID;
 #pragma unroll
-    for (int i = 1; i < NGRID; ++i) {
-        const double vv = i * s.deltav - vhigh;
-        s.vv[i - 1] = vv;
-        s.w[i - 1] = node_weight(lp.kernel, sqrt(vdr2 + vv * vv) / vsmooth);
+        for (int i = 1; i < NGRID; ++i) {
+            const double v = i * deltav - vhigh;
+            vv[i - 1] = v;
+            w[i - 1] = node_weight<double>(lp.kernel, sqrt(vdr2 + v * v) / vsmooth);
+        }
+        const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
+        ampd = amp * (double)in.dens;
+        nbins = lp.nbins;
+        bintov = lp.vbox / nbins;
+        velfac = lp.velfac;
+        zmax = (long long)floor(vel / bintov);
+        return true;
     }
-    const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / s.btherm);
-    s.ampd = amp * (double)in.dens;
-    const double bintov = lp.vbox / lp.nbins;
-    s.zmax = (long long)floor(s.vel / bintov);
-    return true;
-}
 
-// tau_kern_inner, singleabs.h:143-167
-__device__ __forceinline__ double tau_inner(const TauPair &s, double vouter)
-{
-    double total = 0;
+    template <bool COUNT>
+    __device__ __forceinline__ double inner(double vouter, Counters &ct) const
+    {
+        double total = 0;
 #pragma unroll
-    for (int i = 0; i < NGRID - 1; ++i)
-        total += voigt_f64((s.vv[i] - vouter) * s.inv_b, s.aa) * s.w[i];
-    return s.deltav * total;
-}
-
-// tau_kern_outer, singleabs.h:104-126.  A sub-sample count beyond
-// MAX_SUBSAMPLES (b -> 0, where the reference's int conversion overflows)
-// returns NaN and raises DEVERR_WINDOW_LIMIT instead of looping.
-__device__ __forceinline__ double tau_outer(const TauPair &s, double vlow, double vhigh,
-                                           unsigned *dev_err)
-{
-    if ((vhigh - vlow) < s.half_b)
-        return tau_inner(s, (vhigh + vlow) / 2.);
-    const double npd = 2 * ceil((vhigh - vlow) / s.half_b / 2) + 1.;
-    if (!(npd <= MAX_SUBSAMPLES)) {
-        atomicOr(dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
-        return __longlong_as_double(0x7ff8000000000000ll);
+        for (int i = 0; i < NODES; ++i) {
+            const double u = (vv[i] - vouter) * inv_b;
+            if (COUNT) {
+                if (aa == 0.0 || aa > 0.1 || aa < 0.0)
+                    ct.c++;
+                else if (u * u + aa * aa >= 64.0)
+                    ct.b++;
+                else
+                    ct.a++;
+            }
+            total += voigt_f64(u, aa) * w[i];
+        }
+        return deltav * total;
     }
-    const int npoints = (int)npd;
-    double total = tau_inner(s, vlow) / 2.;
-    const double deltav = (vhigh - vlow) / (npoints - 1);
-    for (int i = 1; i < npoints - 1; ++i)
-        total += tau_inner(s, i * deltav + vlow);
-    total += tau_inner(s, vhigh) / 2.;
-    return total / (npoints - 1);
+
+    // tau_kern_outer (singleabs.h:104-126); the sub-sample count is capped.
+    template <bool COUNT>
+    __device__ __forceinline__ double outer(double vlow, double vhigh, unsigned *dev_err,
+                                           Counters &ct) const
+    {
+        if ((vhigh - vlow) < half_b)
+            return inner<COUNT>((vhigh + vlow) / 2., ct);
+        const double npd = 2 * ceil((vhigh - vlow) / half_b / 2) + 1.;
+        if (!(npd <= MAX_SUBSAMPLES)) {
+            atomicOr(dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
+            return nan_d();
+        }
+        const int npoints = (int)npd;
+        double total = inner<COUNT>(vlow, ct) / 2.;
+        const double dv = (vhigh - vlow) / (npoints - 1);
+        for (int i = 1; i < npoints - 1; ++i)
+            total += inner<COUNT>(i * dv + vlow, ct);
+        total += inner<COUNT>(vhigh, ct) / 2.;
+        return total / (npoints - 1);
+    }
+
+    template <bool COUNT>
+    __device__ __forceinline__ double taulast(long long z, unsigned *dev_err, Counters &ct) const
+    {
+        const double vlow = (double)z * bintov - vel;
+        return ampd * outer<COUNT>(vlow, vlow + bintov, dev_err, ct) / velfac;
+    }
+};
+
+// ------------------------------------------------ FP32 (tuned form) pair
+// Profiles with a outside [0, 0.1] (very cold gas, negative damping) use the
+// FP64 profile; kept out of line so the FP32 hot loop stays small.
+__device__ __noinline__ float voigt_wide32(float u, double a)
+{
+    return (float)voigt_f64((double)u, a);
 }
 
-// Upper bound of |taulast| for this pair (any pixel): |amp dens/velfac| x
-// deltav x 7 x max|kernel weight| x max H, H <= 1 for a >= 0.
+struct Tau32 {
+    Voigt32 vc;
+    float U[NODES], w[NODES];   // node velocities / b and kernel weights
+    float inv_b, base0, bintov, hbin_b, scale, sub_dv;
+    float aa_f;
+    double aa_d;
+    long long zmax;
+    int npoints;                 // 1: midpoint; else trapezoid points (uniform per pair)
+    bool wide;                   // a > 0.1 or a < 0: profile evaluated in FP64
+
+    __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
+    {
+        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+        if (hh2 - in.dr2 <= 0)
+            return false;
+        const double btherm = lp.bfac * sqrt((double)in.temp);
+        const double vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
+        const double bintov_d = lp.vbox / lp.nbins;
+        zmax = (long long)floor(vel / bintov_d);
+        base0 = (float)((double)zmax * bintov_d - vel);   // FP64 offset of pixel zmax
+        bintov = (float)bintov_d;
+        const float b = (float)btherm;
+        inv_b = 1.0f / b;
+        aa_d = lp.voigt_fac / btherm;
+        aa_f = (float)aa_d;
+        wide = !(aa_d >= 0.0 && aa_d <= 0.1);
+        vc = make_voigt32(aa_f);
+        const float vdr2 = (float)((lp.velfac * in.dr2) * lp.velfac);
+        const float vsmooth = (float)(lp.velfac * (double)in.smooth);
+        const float vhigh = (vsmooth * vsmooth > vdr2 ? sqrtf(vsmooth * vsmooth - vdr2) : 0.f);
+        const float deltav = 2.f * vhigh / NGRID;
+#pragma unroll
+        for (int i = 1; i < NGRID; ++i) {
+            const float v = (float)i * deltav - vhigh;
+            U[i - 1] = v * inv_b;
+            w[i - 1] = node_weight<float>(lp.kernel, sqrtf(vdr2 + v * v) / vsmooth);
+        }
+        const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
+        // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov)
+        const double half_b = btherm / 2.;
+        double npd = 1.0;
+        if (!(bintov_d < half_b))
+            npd = 2 * ceil(bintov_d / half_b / 2) + 1.;
+        if (!(npd <= MAX_SUBSAMPLES))
+            npd = MAX_SUBSAMPLES + 1;   // flagged in taulast
+        npoints = (int)npd;
+        double sc = amp * (double)in.dens / lp.velfac * (double)deltav;
+        if (npoints > 1)
+            sc /= (npoints - 1);
+        scale = (float)sc;
+        hbin_b = 0.5f * bintov * inv_b;
+        sub_dv = npoints > 1 ? (float)(bintov_d / (npoints - 1)) * inv_b : 0.f;
+        return true;
+    }
+
+    template <bool COUNT>
+    __device__ __forceinline__ float inner(float V, const float2 *tab, Counters &ct) const
+    {
+        float total = 0.f;
+        if (!wide) {
+            unsigned nn = 0;
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                total = fmaf(voigt_f32<COUNT>(U[i] - V, vc, tab, nn), w[i], total);
+            if (COUNT) {
+                ct.a += nn;
+                ct.b += NODES - nn;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                total = fmaf((float)voigt_wide32(U[i] - V, aa_d), w[i], total);
+            if (COUNT)
+                ct.c += NODES;
+        }
+        return total;
+    }
+
+    template <bool COUNT>
+    __device__ __forceinline__ float taulast(long long z, unsigned *dev_err, const float2 *tab,
+                                             Counters &ct) const
+    {
+        const float k = (float)(z - zmax);
+        const float vlow_b = fmaf(k, bintov, base0) * inv_b;   // (v_low - v_particle) / b
+        if (npoints == 1)
+            return scale * inner<COUNT>(vlow_b + hbin_b, tab, ct);
+        if (npoints > (int)MAX_SUBSAMPLES) {
+            atomicOr(dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
+            return __int_as_float(0x7fc00000);
+        }
+        float total = 0.5f * inner<COUNT>(vlow_b, tab, ct);
+        for (int i = 1; i < npoints - 1; ++i)
+            total += inner<COUNT>(fmaf((float)i, sub_dv, vlow_b), tab, ct);
+        total += 0.5f * inner<COUNT>(vlow_b + 2.f * hbin_b, tab, ct);
+        return scale * total;
+    }
+};
+
+// Upper bound of |taulast| for a pair (any pixel): |amp dens/velfac| x deltav x
+// 7 x max|kernel weight| x max H, with H <= 1 for a >= 0.
 __device__ __forceinline__ double tau_pair_bound(const LineParams &lp, const PairInput &in)
 {
     const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
@@ -288,41 +453,61 @@ __device__ __forceinline__ double tau_pair_bound(const LineParams &lp, const Pai
            kernel_max(lp.kernel) * hmax * 1.0001;
 }
 
-struct ColdenPair {
-    double pos1, zrange, hh2;
+// ------------------------------------------------------------ colden pair
+struct Colden {
+    double pos1, zrange, smooth, dr2, boxtokpc;
+    float base_f, box_f, zrange_f, smooth_f, dr2_f, dens_f;
+    double dens;
     long long zlow, zhigh;
-};
+    int kernel;
+    bool ok;   // window within MAX_COLDEN_WINDOW
 
-__device__ __forceinline__ bool colden_setup(const LineParams &lp, const PairInput &in,
-                                             double boxtokpc, ColdenPair &c)
-{
-    c.pos1 = (double)in.ppos;
-    c.hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-    if (c.hh2 - in.dr2 <= 0)
-        return false;   // absorption.cpp:182
-    c.zrange = sqrt(c.hh2 - in.dr2);
-    const double lo = floor((c.pos1 - c.zrange) / boxtokpc);
-    const double hi = ceil((c.pos1 + c.zrange) / boxtokpc);
-    if (!(hi - lo < (double)MAX_COLDEN_WINDOW) || !(fabs(lo) < 9e15) || !(fabs(hi) < 9e15)) {
-        c.zlow = 0;
-        c.zhigh = -1;   // empty window; the caller flags the pair
+    __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in, double btk)
+    {
+        pos1 = (double)in.ppos;
+        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+        if (hh2 - in.dr2 <= 0)
+            return false;   // absorption.cpp:182
+        zrange = sqrt(hh2 - in.dr2);
+        boxtokpc = btk;
+        smooth = (double)in.smooth;
+        dr2 = in.dr2;
+        dens = (double)in.dens;
+        kernel = lp.kernel;
+        const double lo = floor((pos1 - zrange) / boxtokpc);
+        const double hi = ceil((pos1 + zrange) / boxtokpc);
+        ok = (hi - lo < (double)MAX_COLDEN_WINDOW) && fabs(lo) < 9e15 && fabs(hi) < 9e15;
+        zlow = ok ? (long long)lo : 0;
+        zhigh = ok ? (long long)hi : -1;
+        // FP32 form: pixel edges relative to the particle from an FP64 origin
+        base_f = (float)(boxtokpc * (double)zlow - pos1);
+        box_f = (float)boxtokpc;
+        zrange_f = (float)zrange;
+        smooth_f = in.smooth;
+        dr2_f = (float)in.dr2;
+        dens_f = in.dens;
         return true;
     }
-    c.zlow = (long long)lo;
-    c.zhigh = (long long)hi;
-    return true;
-}
 
-__device__ __forceinline__ bool colden_window_ok(const ColdenPair &c)
-{
-    return c.zhigh >= c.zlow;
-}
+    __device__ __forceinline__ double value64(long long z) const
+    {
+        const double plow = (boxtokpc * (double)z - pos1);
+        return dens * kern_frac<double>(kernel, plow, plow + boxtokpc, smooth, dr2, zrange);
+    }
+
+    __device__ __forceinline__ float value32(long long z) const
+    {
+        const float plow = fmaf((float)(z - zlow), box_f, base_f);
+        return dens_f *
+               kern_frac<float>(kernel, plow, plow + box_f, smooth_f, dr2_f, zrange_f);
+    }
+};
 
 __device__ __forceinline__ double colden_pair_bound(const LineParams &lp, const PairInput &in,
                                                     double boxtokpc)
 {
-    ColdenPair c;
-    if (!colden_setup(lp, in, boxtokpc, c))
+    Colden c;
+    if (!c.setup(lp, in, boxtokpc))
         return 0.0;
     const double npix = (double)(c.zhigh - c.zlow + 1);
     const double wraps = ceil(npix / lp.nbins);
@@ -361,43 +546,61 @@ struct DepositArgs {
     int *n_bad;
     unsigned *dev_err;
     unsigned long long *gacc;   // global accumulators when not in shared memory
+    unsigned long long *counters;   // [4] (counting variant only)
     int smem_mode;
     int persistent;
 };
 
-// Walk one tau pair with the whole warp.
-__device__ __forceinline__ void walk_tau(const DepositArgs &a, const TauPair &s, int S,
-                                         unsigned long long *lo, unsigned long long *hi,
-                                         int *bad, int lane)
+template <class R>
+__device__ __forceinline__ void accumulate(const DepositArgs &a, R v, long long z, int S,
+                                           unsigned long long *lo, unsigned long long *hi,
+                                           int *bad)
 {
-    const int nbins = a.lp.nbins;
-    const double bintov = a.lp.vbox / nbins;
-    const long long half = nbins / 2;
-    // forward: z in [zmax, zmax + nbins/2)
+    if (!isfinite(v)) {
+        *bad = 1;
+        return;
+    }
+    unsigned long long l, h;
+    if (to_fixed(v, S, l, h))
+        fixed_add(lo, hi, wrap_bin(z, a.lp.nbins), l, h);
+    else
+        atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+}
+
+// Walk one tau pair with the whole warp: 32 consecutive pixels per step.
+template <int PREC, bool COUNT, class P>
+__device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S,
+                                         unsigned long long *lo, unsigned long long *hi,
+                                         int *bad, int lane, const float2 *tab, Counters &ct)
+{
+    const long long half = a.lp.nbins / 2;
     for (int dir = 0; dir < 2; dir++) {
         const long long start = dir == 0 ? s.zmax : s.zmax - 1;
         for (long long step = 0; step < half; step += 32) {
             const long long k = step + lane;
             const bool valid = k < half;
             const long long z = dir == 0 ? start + k : start - k;
+            Counters c1 = {0, 0, 0, 0};
             double tl = 0.0;
-            bool stop = false;
             if (valid) {
-                const double vlow = (double)z * bintov - s.vel;
-                tl = s.ampd * tau_outer(s, vlow, vlow + bintov, a.dev_err) / a.lp.velfac;
-                stop = tl < a.lp.tautail;
+                if constexpr (PREC == 0)
+                    tl = s.template taulast<COUNT>(z, a.dev_err, c1);
+                else
+                    tl = (double)s.template taulast<COUNT>(z, a.dev_err, tab, c1);
             }
-            const unsigned m = __ballot_sync(0xffffffffu, valid && stop);
+            const bool stop = valid && (tl < a.lp.tautail);
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
             const int last = m ? (__ffs(m) - 1) : 31;
             if (valid && lane <= last) {
-                if (!isfinite(tl)) {
-                    *bad = 1;
-                } else {
-                    unsigned long long l, h;
-                    if (to_fixed(tl, S, l, h))
-                        fixed_add(lo, hi, wrap_bin(z, nbins), l, h);
-                    else
-                        atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+                if constexpr (PREC == 0)
+                    accumulate<double>(a, tl, z, S, lo, hi, bad);
+                else
+                    accumulate<float>(a, (float)tl, z, S, lo, hi, bad);
+                if (COUNT) {
+                    ct.a += c1.a;
+                    ct.b += c1.b;
+                    ct.c += c1.c;
+                    ct.pixels++;
                 }
             }
             if (m)
@@ -406,39 +609,36 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const TauPair &s,
     }
 }
 
-__device__ __forceinline__ void walk_colden(const DepositArgs &a, const PairInput &in,
-                                            const ColdenPair &c, double boxtokpc, int S,
+template <int PREC, bool COUNT>
+__device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &c, int S,
                                             unsigned long long *lo, unsigned long long *hi,
-                                            int *bad, int lane)
+                                            int *bad, int lane, Counters &ct)
 {
-    const int nbins = a.lp.nbins;
     for (long long z = c.zlow + lane; z <= c.zhigh; z += 32) {
-        const double plow = (boxtokpc * (double)z - c.pos1);
-        const double v = (double)in.dens *
-                         kern_frac(a.lp.kernel, plow, plow + boxtokpc, (double)in.smooth, in.dr2,
-                                   c.zrange);
-        if (!isfinite(v)) {
-            *bad = 1;
-        } else {
-            unsigned long long l, h;
-            if (to_fixed(v, S, l, h))
-                fixed_add(lo, hi, wrap_bin(z, nbins), l, h);
-            else
-                atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
-        }
+        if constexpr (PREC == 0)
+            accumulate<double>(a, c.value64(z), z, S, lo, hi, bad);
+        else
+            accumulate<float>(a, c.value32(z), z, S, lo, hi, bad);
+        if (COUNT)
+            ct.pixels++;
     }
 }
 
-template <bool TAU>
-__global__ void __launch_bounds__(256) deposit_kernel(DepositArgs a)
+template <bool TAU, int PREC, bool COUNT>
+__global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
+    deposit_kernel(DepositArgs a)
 {
     extern __shared__ unsigned long long smem[];
     __shared__ double red[32];
+    __shared__ float2 vtab[FSG_V32_N];
     __shared__ int s_bad;
     __shared__ unsigned s_ticket;
     const int nbins = a.lp.nbins;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const double boxtokpc = a.lp.vbox / nbins / a.lp.velfac;
+    Counters ct = {0, 0, 0, 0};
+    if constexpr (PREC == 1 && TAU)
+        stage_voigt32(vtab);
 
     unsigned ticket = blockIdx.x;
     if (a.persistent) {
@@ -478,19 +678,25 @@ __global__ void __launch_bounds__(256) deposit_kernel(DepositArgs a)
         if (!s_bad && B > 0.0) {
             for (long long e = e0 + warp; e < e1; e += nwarps) {
                 const PairInput in = load_pair(a.p, a.pl, e, axis, TAU);
-                if (TAU) {
-                    TauPair s;
-                    if (tau_setup(a.lp, in, s))
-                        walk_tau(a, s, S, lo, hi, &s_bad, lane);
+                if constexpr (TAU) {
+                    if constexpr (PREC == 0) {
+                        Tau64 s;
+                        if (s.setup(a.lp, in))
+                            walk_tau<0, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
+                    } else {
+                        Tau32 s;
+                        if (s.setup(a.lp, in))
+                            walk_tau<1, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
+                    }
                 } else {
-                    ColdenPair c;
-                    if (colden_setup(a.lp, in, boxtokpc, c)) {
-                        if (!colden_window_ok(c)) {
+                    Colden c;
+                    if (c.setup(a.lp, in, boxtokpc)) {
+                        if (!c.ok) {
                             if (lane == 0)
                                 atomicOr(a.dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
                             s_bad = 1;
                         } else {
-                            walk_colden(a, in, c, boxtokpc, S, lo, hi, &s_bad, lane);
+                            walk_colden<PREC, COUNT>(a, c, S, lo, hi, &s_bad, lane, ct);
                         }
                     }
                 }
@@ -514,6 +720,12 @@ __global__ void __launch_bounds__(256) deposit_kernel(DepositArgs a)
         __syncthreads();
         ticket = s_ticket;
     }
+    if constexpr (COUNT) {
+        atomicAdd(&a.counters[0], ct.a);
+        atomicAdd(&a.counters[1], ct.b);
+        atomicAdd(&a.counters[2], ct.c);
+        atomicAdd(&a.counters[3], ct.pixels);
+    }
 }
 
 // Fallback for sightlines with non-finite contributions: FP64 atomics straight
@@ -530,13 +742,13 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
     const double boxtokpc = lp.vbox / nbins / lp.velfac;
     double *row = out + (size_t)line * nbins;
     const long long e0 = pl.off[line], e1 = pl.off[line + 1];
+    Counters ct = {0, 0, 0, 0};
     for (long long e = e0 + warp; e < e1; e += nwarps) {
         const PairInput in = load_pair(p, pl, e, axis, TAU);
         if (TAU) {
-            TauPair s;
-            if (!tau_setup(lp, in, s))
+            Tau64 s;
+            if (!s.setup(lp, in))
                 continue;
-            const double bintov = lp.vbox / nbins;
             const long long half = nbins / 2;
             for (int dir = 0; dir < 2; dir++) {
                 const long long start = dir == 0 ? s.zmax : s.zmax - 1;
@@ -545,13 +757,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
                     const bool valid = k < half;
                     const long long z = dir == 0 ? start + k : start - k;
                     double tl = 0.0;
-                    bool stop = false;
-                    if (valid) {
-                        const double vlow = (double)z * bintov - s.vel;
-                        tl = s.ampd * tau_outer(s, vlow, vlow + bintov, dev_err) / lp.velfac;
-                        stop = tl < lp.tautail;
-                    }
-                    const unsigned m = __ballot_sync(0xffffffffu, valid && stop);
+                    if (valid)
+                        tl = s.taulast<false>(z, dev_err, ct);
+                    const unsigned m = __ballot_sync(0xffffffffu, valid && tl < lp.tautail);
                     const int last = m ? (__ffs(m) - 1) : 31;
                     if (valid && lane <= last)
                         atomicAdd(&row[wrap_bin(z, nbins)], tl);
@@ -560,25 +768,39 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
                 }
             }
         } else {
-            ColdenPair c;
-            if (!colden_setup(lp, in, boxtokpc, c))
+            Colden c;
+            if (!c.setup(lp, in, boxtokpc))
                 continue;
-            if (!colden_window_ok(c)) {
+            if (!c.ok) {
                 if (lane == 0)
                     atomicOr(dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
                 continue;
             }
-            for (long long z = c.zlow + lane; z <= c.zhigh; z += 32) {
-                const double plow = (boxtokpc * (double)z - c.pos1);
-                atomicAdd(&row[wrap_bin(z, nbins)],
-                          (double)in.dens * kern_frac(lp.kernel, plow, plow + boxtokpc,
-                                                      (double)in.smooth, in.dr2, c.zrange));
-            }
+            for (long long z = c.zlow + lane; z <= c.zhigh; z += 32)
+                atomicAdd(&row[wrap_bin(z, nbins)], c.value64(z));
         }
     }
 }
 
 int g_max_smem_optin = -1;
+
+template <bool TAU, int PREC, bool COUNT>
+void launch_one(const DepositArgs &a, int grid, int threads, size_t smem, cudaStream_t s)
+{
+    auto k = deposit_kernel<TAU, PREC, COUNT>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<grid, threads, smem, s>>>(a);
+}
+
+template <bool TAU, int PREC, bool COUNT>
+int resident_ctas(int threads, size_t smem)
+{
+    auto k = deposit_kernel<TAU, PREC, COUNT>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem);
+    return n;
+}
 
 }  // namespace
 
@@ -590,14 +812,25 @@ int deposit_max_smem_bins()
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         g_max_smem_optin = v;
     }
-    // static shared memory of the kernel is < 1 KiB
-    return (g_max_smem_optin - 1024) / 16;
+    // static shared memory of the kernel is < 1.5 KiB
+    return (g_max_smem_optin - 2048) / 16;
+}
+
+int deposit_resident_ctas(int compute_tau, int precision, int threads, int nbins, int smem_mode)
+{
+    const size_t smem = smem_mode ? (size_t)16 * nbins : 0;
+    if (compute_tau)
+        return precision ? resident_ctas<true, 1, false>(threads, smem)
+                         : resident_ctas<true, 0, false>(threads, smem);
+    return precision ? resident_ctas<false, 1, false>(threads, smem)
+                     : resident_ctas<false, 0, false>(threads, smem);
 }
 
 void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
                     const PairLists &pl, const int *line_order, int nlos, double *out,
                     unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
-                    unsigned long long *gacc, const DepositLaunch &cfg, cudaStream_t s)
+                    unsigned long long *gacc, unsigned long long *counters,
+                    const DepositLaunch &cfg, cudaStream_t s)
 {
     if (nlos == 0)
         return;
@@ -614,19 +847,27 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
     a.n_bad = n_bad;
     a.dev_err = dev_err;
     a.gacc = gacc;
+    a.counters = counters;
     a.smem_mode = cfg.smem_mode;
     a.persistent = cfg.persistent;
     const size_t smem = cfg.smem_mode ? (size_t)16 * lp.nbins : 0;
     const int grid = cfg.persistent ? cfg.grid : nlos;
-    const int threads = cfg.threads > 0 ? cfg.threads : 256;
+    const int threads = cfg.threads;
+    const bool count = counters != nullptr;
     if (lp.compute_tau) {
-        cudaFuncSetAttribute(deposit_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        deposit_kernel<true><<<grid, threads, smem, s>>>(a);
+        if (cfg.precision == 0)
+            count ? launch_one<true, 0, true>(a, grid, threads, smem, s)
+                  : launch_one<true, 0, false>(a, grid, threads, smem, s);
+        else
+            count ? launch_one<true, 1, true>(a, grid, threads, smem, s)
+                  : launch_one<true, 1, false>(a, grid, threads, smem, s);
     } else {
-        cudaFuncSetAttribute(deposit_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-        deposit_kernel<false><<<grid, threads, smem, s>>>(a);
+        if (cfg.precision == 0)
+            count ? launch_one<false, 0, true>(a, grid, threads, smem, s)
+                  : launch_one<false, 0, false>(a, grid, threads, smem, s);
+        else
+            count ? launch_one<false, 1, true>(a, grid, threads, smem, s)
+                  : launch_one<false, 1, false>(a, grid, threads, smem, s);
     }
 }
 

@@ -98,15 +98,23 @@ struct DepositLaunch {
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
 // whose contributions are not all finite are appended to bad_lines (counter
 // *n_bad) and left for deposit_fallback.
+// counters (may be null): launches the counting variant, which adds
+// {core-branch evals, wing-branch evals, other evals, pixels} into counters[0..3].
 void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
                     const PairLists &pl, const int *line_order, int nlos, double *out,
                     unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
-                    unsigned long long *gacc, const DepositLaunch &cfg, cudaStream_t s);
+                    unsigned long long *gacc, unsigned long long *counters,
+                    const DepositLaunch &cfg, cudaStream_t s);
+// CTAs of the deposit kernel that fit on one SM for this configuration.
+int deposit_resident_ctas(int compute_tau, int precision, int threads, int nbins, int smem_mode);
 // Plain FP64 atomics into out for the listed lines (non-finite propagation).
 void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Particles &p,
                              const PairLists &pl, const int *bad_lines, int n_bad, double *out,
                              unsigned *dev_err, cudaStream_t s);
 
 int deposit_max_smem_bins();
+
+// Peak FMA throughput of this GPU (TFLOP/s, 2 flops per FMA), own microbenchmark.
+double measure_fma_peak(int precision, cudaStream_t s);
 
 }  // namespace fsg

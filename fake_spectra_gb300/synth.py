@@ -295,3 +295,186 @@ def config4(seed=4, nside=128, nlos=1024):
 
 
 CONFIGS = {0: config0, 1: config1, 2: config2, 3: config3, 4: config4}
+
+
+# ---------------------------------------------------------------------------
+# torch generator for the large workloads (same recipes, built where the data
+# is needed, in seconds).  The random streams differ from the numpy ones, so
+# the two generators give different (equally valid) realisations.  The CIC
+# density is accumulated in 2^-40 fixed point with integer scatter-adds, which
+# makes it independent of the order of the device's atomic updates.
+# ---------------------------------------------------------------------------
+def _t_cic_overdensity(pos, box, ngrid, floor=1e-3, chunk=1 << 24):
+    import torch
+    dev = pos.device
+    n = pos.shape[0]
+    ncell = ngrid ** 3
+    grid = torch.zeros(ncell, dtype=torch.int64, device=dev)
+    scale = ngrid / box
+    one = float(1 << 40)
+
+    def corners(p):
+        u = p * scale - 0.5
+        i0 = torch.floor(u)
+        f = u - i0
+        i0 = torch.remainder(i0.to(torch.int64), ngrid)
+        i1 = torch.remainder(i0 + 1, ngrid)
+        return i0, i1, f
+
+    def loop(i0, i1, f, fn):
+        for cx in (0, 1):
+            ix = i1[:, 0] if cx else i0[:, 0]
+            wx = f[:, 0] if cx else 1.0 - f[:, 0]
+            for cy in (0, 1):
+                iy = i1[:, 1] if cy else i0[:, 1]
+                wy = f[:, 1] if cy else 1.0 - f[:, 1]
+                for cz in (0, 1):
+                    iz = i1[:, 2] if cz else i0[:, 2]
+                    wz = f[:, 2] if cz else 1.0 - f[:, 2]
+                    fn((ix * ngrid + iy) * ngrid + iz, wx * wy * wz)
+
+    for s in range(0, n, chunk):
+        i0, i1, f = corners(pos[s:s + chunk])
+        loop(i0, i1, f, lambda idx, w: grid.index_add_(0, idx, torch.round(w * one).to(torch.int64)))
+    gridf = grid.to(torch.float64) * (ncell / (float(n) * one))
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    for s in range(0, n, chunk):
+        i0, i1, f = corners(pos[s:s + chunk])
+        acc = torch.zeros(i0.shape[0], dtype=torch.float64, device=dev)
+
+        def add(idx, w, acc=acc):
+            acc.add_(gridf[idx] * w)
+        loop(i0, i1, f, add)
+        out[s:s + chunk] = acc
+    return torch.clamp(out, min=floor)
+
+
+def _t_lognormal(g, sigma, n, dev):
+    import torch
+    return torch.exp(sigma * torch.randn(n, generator=g, device=dev, dtype=torch.float64)
+                     - 0.5 * sigma * sigma)
+
+
+@dataclass
+class DeviceWorkload:
+    """A workload whose particle arrays are float32 torch tensors (on any device)."""
+    name: str
+    box: float
+    nbins: int
+    velfac: float
+    atime: float
+    rscale: float
+    kernel: int
+    pos: object
+    vel: object
+    temp: object
+    hh: object
+    dens: Dict[str, object]
+    axis: np.ndarray
+    cofm: np.ndarray
+    transitions: List[Transition] = field(default_factory=list)
+    tautail: float = 1e-7
+
+    @property
+    def npart(self):
+        return int(self.pos.shape[0])
+
+    @property
+    def nlos(self):
+        return int(self.axis.shape[0])
+
+    def call_args(self, transition, compute_tau=True, kernel=None):
+        t = transition
+        return (int(bool(compute_tau)), self.nbins, self.kernel if kernel is None else kernel,
+                self.box, self.velfac, self.atime, t.lambda_cm, t.gamma, t.fosc, t.amumass,
+                self.tautail, self.pos, self.vel, self.dens[t.species], self.temp, self.hh,
+                self.axis, self.cofm)
+
+    def to_host(self):
+        """The same workload with numpy arrays (for the CPU oracle)."""
+        f = lambda x: x.detach().cpu().numpy()
+        return Workload(name=self.name, box=self.box, nbins=self.nbins, velfac=self.velfac,
+                        atime=self.atime, rscale=self.rscale, kernel=self.kernel,
+                        pos=f(self.pos), vel=f(self.vel), temp=f(self.temp), hh=f(self.hh),
+                        dens={k: f(v) for k, v in self.dens.items()}, axis=self.axis,
+                        cofm=self.cofm, transitions=list(self.transitions),
+                        tautail=self.tautail)
+
+
+def generate_torch(config, seed=None, device="cuda", nside=None, nlos=None):
+    """Config 1-4 recipes with torch random streams, arrays on `device`."""
+    import torch
+    spec = {
+        1: dict(box=6e4, nside=256, res=1.0, frac=0.3, nclumps=2000, sigma=100.0, sigma_ln=None,
+                lines=[LYA], grid=(60, 3), seed=1),
+        2: dict(box=6e4, nside=256, res=1.0, frac=0.3, nclumps=2000, sigma=100.0, sigma_ln=None,
+                lines=[LYA, LYB, CIV], grid=(60, 3), seed=2),
+        3: dict(box=1e5, nside=512, res=1.0, frac=0.4, nclumps=20000, sigma=150.0, sigma_ln=0.5,
+                lines=[LYA, LYB, CIV], nlos=32768, seed=3),
+        4: dict(box=2e4, nside=128, res=2.0, frac=0.3, nclumps=250, sigma=100.0, sigma_ln=None,
+                lines=[LYA], nlos=1024, seed=4),
+    }[config]
+    seed = spec["seed"] if seed is None else seed
+    full_side = spec["nside"]
+    nside = nside or full_side
+    box = spec["box"]
+    n = nside ** 3
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    dev = torch.device(device)
+    f64 = torch.float64
+    nclumps = max(1, int(round(spec["nclumps"] * (nside / full_side) ** 3)))
+    centres = torch.rand(nclumps, 3, generator=g, device=dev, dtype=f64) * box
+    if spec["sigma_ln"] is None:
+        widths = torch.full((nclumps,), spec["sigma"], device=dev, dtype=f64)
+    else:
+        widths = spec["sigma"] * torch.exp(spec["sigma_ln"] * torch.randn(
+            nclumps, generator=g, device=dev, dtype=f64))
+    ncl = int(round(spec["frac"] * n))
+    pos = torch.empty(n, 3, device=dev, dtype=f64)
+    pos[:n - ncl] = torch.rand(n - ncl, 3, generator=g, device=dev, dtype=f64) * box
+    which = torch.randint(0, nclumps, (ncl,), generator=g, device=dev)
+    pos[n - ncl:] = centres[which] + widths[which, None] * torch.randn(
+        ncl, 3, generator=g, device=dev, dtype=f64)
+    del which
+    pos = torch.remainder(pos, box)
+    pos = pos[torch.randperm(n, generator=g, device=dev)]
+    delta1 = _t_cic_overdensity(pos, box, nside // 2)
+    n_hi = 1e-10 * delta1 ** 1.6
+    temp = 1e4 * delta1 ** 0.5 * _t_lognormal(g, 0.3, n, dev)
+    vel = 50.0 * torch.randn(n, 3, generator=g, device=dev, dtype=f64)
+    hh = 2.0 * (box / nside) * delta1 ** (-1.0 / 3.0)
+    dens64 = {"HI": n_hi}
+    if any(t.species == "CIV" for t in spec["lines"]):
+        dens64["CIV"] = 10 ** -4.5 * n_hi * delta1 ** 0.3
+    del delta1
+    rng = np.random.default_rng(seed)
+    if "grid" in spec:
+        axis, cofm = grid_sightlines(spec["grid"][0], spec["grid"][1], box)
+    else:
+        nl = nlos or spec["nlos"]
+        if config == 3:
+            base = nl // 3
+            counts = [base + (1 if i < nl - 3 * base else 0) for i in range(3)]
+            axis = np.concatenate([np.full(c, a + 1, dtype=np.int32) for a, c in enumerate(counts)])
+            cofm = rng.uniform(0.0, box, size=(nl, 3))
+            through = rng.random(nl) < 0.25
+            cen = centres.cpu().numpy()
+            pick = rng.integers(0, nclumps, size=nl)
+            cofm[through] = cen[pick[through]]
+        else:
+            axis, cofm = random_sightlines(rng, nl, 1, box)
+            cofm[:, 0] = 0.0
+    atime, rscale, velfac = cosmology()
+    nbins = int(box * velfac / spec["res"])
+    pos32 = pos.to(torch.float32)
+    pos32[pos32 >= box] = float(np.nextafter(np.float32(box), np.float32(0)))
+    del pos
+    name = "config%d_%dcube_L%g_%dlos_%gkms" % (config, nside, box, len(axis), spec["res"])
+    return DeviceWorkload(
+        name=name, box=float(box), nbins=nbins, velfac=float(velfac), atime=float(atime),
+        rscale=float(rscale), kernel=1, pos=pos32.contiguous(), vel=vel.to(torch.float32),
+        temp=temp.to(torch.float32), hh=hh.to(torch.float32),
+        dens={k: (v * rscale).to(torch.float32) for k, v in dens64.items()},
+        axis=np.asarray(axis, dtype=np.int32), cofm=np.asarray(cofm, dtype=np.float64),
+        transitions=list(spec["lines"]))

@@ -40,10 +40,13 @@ typedef enum {
 
 typedef struct {
     int precision;  /* fsg_precision                                         */
-    int threads;    /* threads per deposit CTA; 0 = default/autotuned        */
+    int threads;    /* threads per deposit CTA; 0 = default                  */
     int persistent; /* -1 = default, 0 = one CTA per sightline, 1 = resident
                        CTAs draining a sightline queue                        */
-    int reserved[5];
+    int count_work; /* 1 = run the counting variant of the deposit and report
+                       the algorithmic work in fsg_stats (slower; for the
+                       roofline only)                                         */
+    int reserved[4];
 } fsg_options;
 
 typedef struct {
@@ -53,12 +56,24 @@ typedef struct {
     int32_t reserved;
     double ms_search;        /* device time of the last pair search            */
     double ms_deposit;       /* device time of the last deposit                */
+    /* Work of the last deposit when count_work was set: Voigt-profile
+     * evaluations by branch and pixel contributions, for the pixels the
+     * reference's tautail window rule evaluates (absorption.cpp:250-278). */
+    int64_t evals_core;      /* FP64: Taylor branch; FP32: |u| < 6 branch      */
+    int64_t evals_wing;      /* asymptotic branch                               */
+    int64_t evals_other;     /* a == 0, a < 0 or a > 0.1 (FP32: FP64 profile)   */
+    int64_t pixels;          /* pixel contributions                             */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
 
 /* Library version string. */
 const char *fsg_version(void);
+
+/* Peak FMA throughput of the current GPU in TFLOP/s (2 flops per FMA) for
+ * precision FSG_PREC_FP64 or FSG_PREC_FP32, from this library's own
+ * microbenchmark; the roofline denominator of the compute-bound deposit. */
+int fsg_measure_fma_peak(int precision, double *tflops, char *errbuf, size_t errlen);
 
 /* Context: one device, one stream, a grow-only device workspace and the pair
  * lists of the last search. */

@@ -20,7 +20,9 @@ def lib():
 
 def header_symbols():
     text = open(os.path.join(ROOT, "include", "fsg.h")).read()
-    return sorted(set(re.findall(r"\b(fsg_[a-z_0-9]+)\s*\(", text)))
+    # declarations: "<type> [*]fsg_name(" at the start of a line
+    decl = re.compile(r"^(?:const\s+)?[a-z_0-9]+\s*\*?\s*(fsg_[a-z_0-9]+)\s*\(", re.M)
+    return sorted(set(decl.findall(text)))
 
 
 def test_header_declares_entry_points():
