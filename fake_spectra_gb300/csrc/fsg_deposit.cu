@@ -348,6 +348,7 @@ struct Tau32 {
     long long zmax;
     int npoints;                 // 1: midpoint; else trapezoid points (uniform per pair)
     bool wide;                   // a > 0.1 or a < 0: profile evaluated in FP64
+    bool careful;                // b far below the pixel or smoothing width: FP64 pair walk
 
     __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
     {
@@ -385,6 +386,9 @@ struct Tau32 {
         if (!(npd <= MAX_SUBSAMPLES))
             npd = MAX_SUBSAMPLES + 1;   // flagged in taulast
         npoints = (int)npd;
+        // Float node offsets U_i = v_i / b keep ~1e-5 absolute accuracy only while
+        // |U_i| <= 256; sub-sampled or very narrow profiles take the FP64 walk.
+        careful = wide || npoints > 8 || (double)vhigh > 256.0 * btherm;
         double sc = amp * (double)in.dens / lp.velfac * (double)deltav;
         if (npoints > 1)
             sc /= (npoints - 1);
@@ -454,11 +458,43 @@ __device__ __forceinline__ double tau_pair_bound(const LineParams &lp, const Pai
 }
 
 // ------------------------------------------------------------ colden pair
+// FP32 form of kern_frac for a pixel lying wholly inside the kernel support
+// [-zrange, zrange].  Node q values come from the distance d of the node to
+// the nearer support edge, anchored in FP64 per pair, so the kernel tails
+// (1-q)^3 and (1-q)^5 keep full relative accuracy:
+//   1 - q^2 = d (2 zrange - d) / h^2 + (1 - hh2/h^2),   1 - q = (1 - q^2)/(1 + q),
+// (hh2 = h*h in float, as the reference forms zrange = sqrt(hh2 - dr2)).
+__device__ __forceinline__ float spline_from_eps(bool cubic, float eps)
+{
+    if (!(eps > 0.f))
+        return 0.f;                                  // q >= 1
+    const float q2 = fmaxf(1.f - eps, 0.f);
+    const float q = sqrtf(q2);
+    const float t = eps / (1.f + q);                 // 1 - q without cancellation
+    if (cubic) {
+        const float norm = (float)(32. / 4 / PI_D);
+        if (q < 0.5f)
+            return norm * (1.f - 6.f * q2 + 6.f * q2 * q);
+        return norm * (2.f * t * t * t);
+    }
+    const float norm = (float)(9. / 40 / PI_D);
+    if (q < (float)(1. / 3)) {
+        const float q4 = q2 * q2;
+        return norm * 6.f * (11.f - 90.f * q2 + 405.f * q4 - 405.f * q4 * q);
+    }
+    const float a = 3.f * t, a2 = a * a;
+    if (q < (float)(2. / 3)) {
+        const float b = a - 1.f, b2 = b * b;
+        return norm * (a2 * a2 * a - 6.f * b2 * b2 * b);
+    }
+    const float t2 = t * t;
+    return norm * (243.f * t2 * t2 * t);
+}
+
 struct Colden {
-    double pos1, zrange, smooth, dr2, boxtokpc;
-    float base_f, box_f, zrange_f, smooth_f, dr2_f, dens_f;
-    double dens;
-    long long zlow, zhigh;
+    double pos1, zrange, smooth, dr2, boxtokpc, dens;
+    float box_f, dL0, dR0, two_zr, inv_h2, ch, dens_f;
+    long long zlow, zhigh, kmax;
     int kernel;
     bool ok;   // window within MAX_COLDEN_WINDOW
 
@@ -479,12 +515,15 @@ struct Colden {
         ok = (hi - lo < (double)MAX_COLDEN_WINDOW) && fabs(lo) < 9e15 && fabs(hi) < 9e15;
         zlow = ok ? (long long)lo : 0;
         zhigh = ok ? (long long)hi : -1;
-        // FP32 form: pixel edges relative to the particle from an FP64 origin
-        base_f = (float)(boxtokpc * (double)zlow - pos1);
+        kmax = zhigh - zlow;
+        // FP32 form: edge distances anchored in FP64 at both ends of the window
         box_f = (float)boxtokpc;
-        zrange_f = (float)zrange;
-        smooth_f = in.smooth;
-        dr2_f = (float)in.dr2;
+        dL0 = (float)(boxtokpc * (double)zlow - pos1 + zrange);    // pixel zlow edge - (-zrange)
+        dR0 = (float)(zrange + pos1 - boxtokpc * (double)zhigh);   // zrange - pixel zhigh edge
+        two_zr = (float)(2.0 * zrange);
+        const double h2 = smooth * smooth;
+        inv_h2 = (float)(1.0 / h2);
+        ch = (float)((h2 - hh2) / h2);
         dens_f = in.dens;
         return true;
     }
@@ -497,9 +536,25 @@ struct Colden {
 
     __device__ __forceinline__ float value32(long long z) const
     {
-        const float plow = fmaf((float)(z - zlow), box_f, base_f);
-        return dens_f *
-               kern_frac<float>(kernel, plow, plow + box_f, smooth_f, dr2_f, zrange_f);
+        const long long k = z - zlow;
+        // the first and the last two pixels may be clipped by the support: FP64
+        if (k == 0 || k >= kmax - 1)
+            return (float)value64(z);
+        if (kernel != SPH_CUBIC && kernel != SPH_QUINTIC)
+            return dens_f * ((float)(3. / 4. / PI_D) * box_f);
+        const bool cubic = (kernel == SPH_CUBIC);
+        const float dz = box_f * (1.f / NGRID);
+        const float l0 = fmaf((float)k, box_f, dL0);
+        const float r0 = fmaf((float)(kmax - k), box_f, dR0);
+        float total = 0.f;
+#pragma unroll
+        for (int i = 0; i <= NGRID; i++) {
+            const float d = fminf(fmaf((float)i, dz, l0), fmaf(-(float)i, dz, r0));
+            const float eps = fmaf(d * (two_zr - d), inv_h2, ch);
+            const float kv = spline_from_eps(cubic, eps);
+            total += (i == 0 || i == NGRID) ? 0.5f * kv : kv;
+        }
+        return dens_f * (dz * total);
     }
 };
 
@@ -624,6 +679,24 @@ __device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &
     }
 }
 
+// Rare pairs of the FP32 form (see Tau32::careful) walk with the FP64 pair;
+// their evaluations count as "other" work.
+template <bool COUNT>
+__device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairInput &in, int S,
+                                              unsigned long long *lo, unsigned long long *hi,
+                                              int *bad, int lane, Counters &ct)
+{
+    Tau64 s;
+    if (!s.setup(a.lp, in))
+        return;
+    Counters c = {0, 0, 0, 0};
+    walk_tau<0, COUNT>(a, s, S, lo, hi, bad, lane, nullptr, c);
+    if (COUNT) {
+        ct.c += c.a + c.b + c.c;
+        ct.pixels += c.pixels;
+    }
+}
+
 template <bool TAU, int PREC, bool COUNT>
 __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     deposit_kernel(DepositArgs a)
@@ -685,8 +758,12 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
                             walk_tau<0, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
                     } else {
                         Tau32 s;
-                        if (s.setup(a.lp, in))
-                            walk_tau<1, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
+                        if (s.setup(a.lp, in)) {
+                            if (s.careful)
+                                walk_tau_careful<COUNT>(a, in, S, lo, hi, &s_bad, lane, ct);
+                            else
+                                walk_tau<1, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
+                        }
                     }
                 } else {
                     Colden c;
