@@ -33,6 +33,7 @@ EXPORTS = (
     "fsg_particle_interpolate_device",
     "fsg_build_pairs_device",
     "fsg_copy_pairs",
+    "fsg_particle_interpolate_noalloc",
 )
 
 _c_int = ctypes.c_int
@@ -111,6 +112,9 @@ def load(path=None):
         L.fsg_build_pairs_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32,
                                              ctypes.POINTER(_c_i64), _p, _c_size]
         L.fsg_copy_pairs.argtypes = [_p, _p, _p, _p, _c_int, _p, _c_size]
+        L.fsg_particle_interpolate_noalloc.argtypes = ([_c_int, _c_int, _c_int] + [_c_d] * 8 +
+                                                       [_p] * 5 + [_c_i64, _p, _p, _c_i32, _p,
+                                                                   _c_int, _p, _p, _c_size])
         _lib = L
         return L
 

@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libfsg.so")
 
-SOURCES = ["fsg_capi.cu", "fsg_index.cu", "fsg_deposit.cu", "fsg_peak.cu"]
+SOURCES = ["fsg_capi.cu", "fsg_index.cu", "fsg_deposit.cu", "fsg_peak.cu", "fsg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -130,6 +130,30 @@ int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const
 int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr2, int sorted,
                    char *errbuf, size_t errlen);
 
+/*
+ * The same interpolation with NO device memory allocation, for callers that
+ * cannot call cudaMalloc (their host application's allocator owns the GPU
+ * memory, or they run inside a loop that must not trigger the synchronisation
+ * an allocation may imply).  This entry point has no counterpart in the
+ * reference.  pos/vel/dens/temp/h/out are DEVICE pointers, axis/cofm HOST
+ * pointers, stream a cudaStream_t (NULL = the default stream); precision is an
+ * fsg_precision.  All scratch lives in one 64 MiB file-scope device array that
+ * every GPU loading the library keeps until exit.  Limits: nlos <= 8192, about
+ * 5.4 million sightline-particle pairs, nbins within the shared-memory
+ * capacity (~14000 on GB300); larger calls return FSG_ERR_VALUE.  The first
+ * call on a device looks up the array's address (do it before any stream
+ * capture).  Calls share the array: they are serialised by a lock and complete
+ * before returning; GPU work overlapping a call on the same array would race.
+ */
+int fsg_particle_interpolate_noalloc(int compute_tau, int nbins, int kernel, double box,
+                                     double velfac, double atime, double lambda, double gamma,
+                                     double fosc, double amumass, double tautail,
+                                     const float *pos, const float *vel, const float *dens,
+                                     const float *temp, const float *h, int64_t npart,
+                                     const int32_t *axis, const double *cofm, int32_t nlos,
+                                     double *out, int precision, void *stream, char *errbuf,
+                                     size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
