@@ -72,7 +72,7 @@ struct fsg_context {
     cudaStream_t stream = nullptr;
     // workspace
     DevBuf pos, vel, dens, temp, hh, out;                    // staging for host-pointer calls
-    DevBuf key, second, axis, cell_start[3], cell_line[3];   // sightline tables
+    DevBuf key, second, axis, pack, cell_start[3], cell_line[3];   // sightline tables
     DevBuf line_count, cursor, off, part, dr2, line_order;   // pair lists
     DevBuf ticket, bad, nbad, err, gacc, counters;           // deposit bookkeeping
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -102,7 +102,7 @@ struct fsg_context {
 
     void release_all()
     {
-        DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis,
+        DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis, &pack,
                           &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
                           &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters};
@@ -196,9 +196,15 @@ void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int n
         G.cell_start = (const int *)cs;
         G.cell_line = (const int *)cl;
     }
+    std::vector<float4> pk(nlos);
+    for (int i = 0; i < nlos; i++)
+        pk[i] = pack_line(key[i], second[i], axis[i]);
     void *dk = c->ensure(c->key, sizeof(double) * nlos);
     void *ds = c->ensure(c->second, sizeof(double) * nlos);
     void *da = c->ensure(c->axis, sizeof(int) * nlos);
+    void *dp = c->ensure(c->pack, sizeof(float4) * nlos);
+    cuda_check(cudaMemcpyAsync(dp, pk.data(), sizeof(float4) * nlos, cudaMemcpyHostToDevice, s),
+               "upload sightlines");
     cuda_check(cudaMemcpyAsync(dk, key.data(), sizeof(double) * nlos, cudaMemcpyHostToDevice, s),
                "upload sightlines");
     cuda_check(cudaMemcpyAsync(ds, second.data(), sizeof(double) * nlos, cudaMemcpyHostToDevice,
@@ -209,6 +215,9 @@ void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int n
     t.key = (const double *)dk;
     t.second = (const double *)ds;
     t.axis = (const int *)da;
+    t.pack = (const float4 *)dp;
+    t.box_f = (float)box;
+    t.pre_eps = prefilter_eps(box);
     c->nlos = nlos;
 }
 

@@ -33,6 +33,8 @@
 #include "fsg_internal.cuh"
 #include "fsg_voigt.cuh"
 
+#include <type_traits>
+
 namespace fsg {
 
 namespace {
@@ -323,10 +325,11 @@ struct Tau64 {
         return total / (npoints - 1);
     }
 
+    // pixel z = zmax + koff
     template <bool COUNT>
-    __device__ __forceinline__ double taulast(long long z, unsigned *dev_err, Counters &ct) const
+    __device__ __forceinline__ double taulast(int koff, unsigned *dev_err, Counters &ct) const
     {
-        const double vlow = (double)z * bintov - vel;
+        const double vlow = (double)(zmax + koff) * bintov - vel;
         return ampd * outer<COUNT>(vlow, vlow + bintov, dev_err, ct) / velfac;
     }
 };
@@ -398,15 +401,41 @@ struct Tau32 {
         return true;
     }
 
+    // Called by every lane of the warp (lanes past the window compute and
+    // discard), so the warp votes below see a converged warp.
     template <bool COUNT>
     __device__ __forceinline__ float inner(float V, const float2 *tab, Counters &ct) const
     {
         float total = 0.f;
         if (!wide) {
+            float u[NODES];
+            bool wing = true, core = true;
+#pragma unroll
+            for (int i = 0; i < NODES; ++i) {
+                u[i] = U[i] - V;
+                wing &= fabsf(u[i]) >= 6.5f;
+                core &= fabsf(u[i]) < 6.0f;
+            }
+            if (__all_sync(0xffffffffu, wing)) {
+#pragma unroll
+                for (int i = 0; i < NODES; ++i)
+                    total = fmaf(voigt_wing32(u[i], vc), w[i], total);
+                if (COUNT)
+                    ct.b += NODES;
+                return total;
+            }
+            if (__all_sync(0xffffffffu, core)) {
+#pragma unroll
+                for (int i = 0; i < NODES; ++i)
+                    total = fmaf(voigt_core32(u[i], vc, tab), w[i], total);
+                if (COUNT)
+                    ct.a += NODES;
+                return total;
+            }
             unsigned nn = 0;
 #pragma unroll
             for (int i = 0; i < NODES; ++i)
-                total = fmaf(voigt_f32<COUNT>(U[i] - V, vc, tab, nn), w[i], total);
+                total = fmaf(voigt_f32<COUNT>(u[i], vc, tab, nn), w[i], total);
             if (COUNT) {
                 ct.a += nn;
                 ct.b += NODES - nn;
@@ -421,11 +450,12 @@ struct Tau32 {
         return total;
     }
 
+    // pixel z = zmax + koff
     template <bool COUNT>
-    __device__ __forceinline__ float taulast(long long z, unsigned *dev_err, const float2 *tab,
+    __device__ __forceinline__ float taulast(int koff, unsigned *dev_err, const float2 *tab,
                                              Counters &ct) const
     {
-        const float k = (float)(z - zmax);
+        const float k = (float)koff;
         const float vlow_b = fmaf(k, bintov, base0) * inv_b;   // (v_low - v_particle) / b
         if (npoints == 1)
             return scale * inner<COUNT>(vlow_b + hbin_b, tab, ct);
@@ -607,7 +637,7 @@ struct DepositArgs {
 };
 
 template <class R>
-__device__ __forceinline__ void accumulate(const DepositArgs &a, R v, long long z, int S,
+__device__ __forceinline__ void accumulate(const DepositArgs &a, R v, int j, int S,
                                            unsigned long long *lo, unsigned long long *hi,
                                            int *bad)
 {
@@ -617,40 +647,54 @@ __device__ __forceinline__ void accumulate(const DepositArgs &a, R v, long long 
     }
     unsigned long long l, h;
     if (to_fixed(v, S, l, h))
-        fixed_add(lo, hi, wrap_bin(z, a.lp.nbins), l, h);
+        fixed_add(lo, hi, j, l, h);
     else
         atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
 }
 
+// bin of pixel zmax + koff from j0 = bin of zmax, |koff| <= nbins
+__device__ __forceinline__ int bin_from(int j0, int koff, int nbins)
+{
+    int j = j0 + koff;
+    if (j < 0)
+        j += nbins;
+    else if (j >= nbins)
+        j -= nbins;
+    return j;
+}
+
 // Walk one tau pair with the whole warp: 32 consecutive pixels per step.
+// Pixel offsets from zmax and bins are int32; the FP32 form compares its float
+// contribution with tautail in float, so no FP64 work is done per pixel.
 template <int PREC, bool COUNT, class P>
 __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S,
                                          unsigned long long *lo, unsigned long long *hi,
                                          int *bad, int lane, const float2 *tab, Counters &ct)
 {
-    const long long half = a.lp.nbins / 2;
+    using R = typename std::conditional<PREC == 0, double, float>::type;
+    const int nbins = a.lp.nbins;
+    const int half = nbins / 2;
+    const R tautail = (R)a.lp.tautail;
+    const int j0 = wrap_bin(s.zmax, nbins);
     for (int dir = 0; dir < 2; dir++) {
-        const long long start = dir == 0 ? s.zmax : s.zmax - 1;
-        for (long long step = 0; step < half; step += 32) {
-            const long long k = step + lane;
+        for (int step = 0; step < half; step += 32) {
+            const int k = step + lane;
             const bool valid = k < half;
-            const long long z = dir == 0 ? start + k : start - k;
+            const int koff = dir == 0 ? k : -1 - k;
             Counters c1 = {0, 0, 0, 0};
-            double tl = 0.0;
-            if (valid) {
-                if constexpr (PREC == 0)
-                    tl = s.template taulast<COUNT>(z, a.dev_err, c1);
-                else
-                    tl = (double)s.template taulast<COUNT>(z, a.dev_err, tab, c1);
+            R tl = (R)0;
+            if constexpr (PREC == 0) {
+                if (valid)
+                    tl = s.template taulast<COUNT>(koff, a.dev_err, c1);
+            } else {
+                // every lane evaluates (warp-uniform fast paths vote inside)
+                tl = s.template taulast<COUNT>(koff, a.dev_err, tab, c1);
             }
-            const bool stop = valid && (tl < a.lp.tautail);
+            const bool stop = valid && (tl < tautail);
             const unsigned m = __ballot_sync(0xffffffffu, stop);
             const int last = m ? (__ffs(m) - 1) : 31;
             if (valid && lane <= last) {
-                if constexpr (PREC == 0)
-                    accumulate<double>(a, tl, z, S, lo, hi, bad);
-                else
-                    accumulate<float>(a, (float)tl, z, S, lo, hi, bad);
+                accumulate<R>(a, tl, bin_from(j0, koff, nbins), S, lo, hi, bad);
                 if (COUNT) {
                     ct.a += c1.a;
                     ct.b += c1.b;
@@ -669,11 +713,15 @@ __device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &
                                             unsigned long long *lo, unsigned long long *hi,
                                             int *bad, int lane, Counters &ct)
 {
-    for (long long z = c.zlow + lane; z <= c.zhigh; z += 32) {
+    const int nbins = a.lp.nbins;
+    const int j0 = wrap_bin(c.zlow, nbins);
+    const int kmax = (int)c.kmax;   // < MAX_COLDEN_WINDOW
+    for (int k = lane; k <= kmax; k += 32) {
+        const int j = (int)(((long long)j0 + k) % nbins);
         if constexpr (PREC == 0)
-            accumulate<double>(a, c.value64(z), z, S, lo, hi, bad);
+            accumulate<double>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
         else
-            accumulate<float>(a, c.value32(z), z, S, lo, hi, bad);
+            accumulate<float>(a, c.value32(c.zlow + k), j, S, lo, hi, bad);
         if (COUNT)
             ct.pixels++;
     }
@@ -826,20 +874,20 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
             Tau64 s;
             if (!s.setup(lp, in))
                 continue;
-            const long long half = nbins / 2;
+            const int half = nbins / 2;
+            const int j0 = wrap_bin(s.zmax, nbins);
             for (int dir = 0; dir < 2; dir++) {
-                const long long start = dir == 0 ? s.zmax : s.zmax - 1;
-                for (long long step = 0; step < half; step += 32) {
-                    const long long k = step + lane;
+                for (int step = 0; step < half; step += 32) {
+                    const int k = step + lane;
                     const bool valid = k < half;
-                    const long long z = dir == 0 ? start + k : start - k;
+                    const int koff = dir == 0 ? k : -1 - k;
                     double tl = 0.0;
                     if (valid)
-                        tl = s.taulast<false>(z, dev_err, ct);
+                        tl = s.taulast<false>(koff, dev_err, ct);
                     const unsigned m = __ballot_sync(0xffffffffu, valid && tl < lp.tautail);
                     const int last = m ? (__ffs(m) - 1) : 31;
                     if (valid && lane <= last)
-                        atomicAdd(&row[wrap_bin(z, nbins)], tl);
+                        atomicAdd(&row[bin_from(j0, koff, nbins)], tl);
                     if (m)
                         break;
                 }

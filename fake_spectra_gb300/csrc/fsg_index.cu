@@ -80,14 +80,30 @@ __device__ __forceinline__ double calc_dr2(double d1, double d2, double box)
 
 // The reference predicate for (particle, line).  `first` is the particle's
 // coordinate for the table the line is in; pos3 the particle position.
+// A float prefilter rejects candidates whose minimum-image distance exceeds
+// hh by more than the float error bound (pre_eps, 4 ulp of the box) before the
+// exact FP64 test: a strict superset of the accepted set, so the result is
+// unchanged while most candidates cost FP32 work only (FP64 runs at 1/64 of the
+// FP32 rate on this GPU).
 __device__ __forceinline__ bool accept(const LineTables &t, int line, const Window &w,
                                        float first, const float *pos3, float hh, double *dr2_out)
 {
+    const float4 pk = __ldg(&t.pack[line]);
+    const int ax = __float_as_int(pk.z);
+    const float second = (ax == 3) ? pos3[1] : pos3[2];
+    {
+        float d1 = fabsf(first - pk.x), d2 = fabsf(second - pk.y);
+        if (d1 <= t.box_f && d2 <= t.box_f && hh > 0.0f) {
+            d1 = fminf(d1, t.box_f - d1);
+            d2 = fminf(d2, t.box_f - d2);
+            const float lim = hh + t.pre_eps;
+            if (fmaf(d1, d1, d2 * d2) > lim * lim * 1.000001f)
+                return false;
+        }
+    }
     const double key = t.key[line];
     if (!in_window(w, key))
         return false;
-    const int ax = t.axis[line];
-    const float second = (ax == 3) ? pos3[1] : pos3[2];
     const double lproj2 = t.second[line];
     if (!second_close(second, lproj2, hh, t.box))
         return false;

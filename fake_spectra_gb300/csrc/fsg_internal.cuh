@@ -14,6 +14,22 @@
 
 namespace fsg {
 
+inline float __int_as_float_host(int i)
+{
+    float f;
+    static_assert(sizeof f == sizeof i, "int/float size");
+    __builtin_memcpy(&f, &i, sizeof f);
+    return f;
+}
+
+// Absolute slack of the float prefilter of the sightline search: the float
+// minimum-image distance differs from the double one by at most ~2 ulp(box).
+inline float prefilter_eps(double box)
+{
+    const float b = (float)box;
+    return 4.0f * (__builtin_nextafterf(b, 2.0f * b + 1.0f) - b) + 1e-30f;
+}
+
 // kernel ids, fake_spectra/singleabs.h:9-12
 enum KernelId { TOP_HAT = 0, SPH_CUBIC = 1, VORONOI = 2, SPH_QUINTIC = 3 };
 
@@ -45,11 +61,25 @@ struct LineTables {
     const double *key;       // index_table.cpp:12-14: cofm[3i+1] (axis 1) or cofm[3i] (axes 2, 3)
     const double *second;    // index_table.cpp:33-39: cofm[3i+1] (axis 3) or cofm[3i+2]
     const int *axis;         // 1-based
+    const float4 *pack;      // per line {key, second, axis bits, 0} in float (prefilter)
     int nlos;
     int n_main;              // lines with axis != 1 (the reference's index_table)
     int n_xx;                // lines with axis == 1 (the reference's index_table_xx)
     double box;
+    float box_f;
+    float pre_eps;           // absolute slack of the float prefilter (4 ulp of the box)
 };
+
+// Float copy of the sightline tables for the search prefilter.
+inline float4 pack_line(double key, double second, int axis)
+{
+    float4 v;
+    v.x = (float)key;
+    v.y = (float)second;
+    v.z = __int_as_float_host(axis);
+    v.w = 0.f;
+    return v;
+}
 
 struct Particles {
     const float *pos;        // [3N]

@@ -51,6 +51,7 @@ void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
 
 // host staging (static: no heap use)
 double h_key[NOALLOC_MAX_LINES], h_second[NOALLOC_MAX_LINES];
+float4 h_pack[NOALLOC_MAX_LINES];
 int h_group[3][NOALLOC_MAX_LINES];
 int h_cell_of[NOALLOC_MAX_LINES];
 int h_cell_start[3][NOALLOC_MAX_NC * NOALLOC_MAX_NC + 1];
@@ -175,6 +176,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
         const int a = axis[i];
         h_key[i] = (a == 1) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i];
         h_second[i] = (a == 3) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i + 2];
+        h_pack[i] = pack_line(h_key[i], h_second[i], a);
         h_group[a - 1][ng[a - 1]++] = i;
     }
     t.n_xx = ng[0];
@@ -183,6 +185,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     double *d_key = (double *)cv.take(sizeof(double) * nlos);
     double *d_second = (double *)cv.take(sizeof(double) * nlos);
     int *d_axis = (int *)cv.take(sizeof(int) * nlos);
+    float4 *d_pack = (float4 *)cv.take(sizeof(float4) * nlos);
     for (int g = 0; g < 3; g++) {
         LineGroup &G = t.g[g];
         const int n = ng[g];
@@ -246,9 +249,14 @@ extern "C" int fsg_particle_interpolate_noalloc(
                             s), "upload sightlines");
     NA_CUDA(cudaMemcpyAsync(d_axis, axis, sizeof(int) * nlos, cudaMemcpyHostToDevice, s),
             "upload sightlines");
+    NA_CUDA(cudaMemcpyAsync(d_pack, h_pack, sizeof(float4) * nlos, cudaMemcpyHostToDevice, s),
+            "upload sightlines");
     t.key = d_key;
     t.second = d_second;
     t.axis = d_axis;
+    t.pack = d_pack;
+    t.box_f = (float)box;
+    t.pre_eps = prefilter_eps(box);
 
     // ---- pair search: count, prefix sum, emit
     Particles p{pos, compute_tau ? vel : nullptr, dens, compute_tau ? temp : nullptr, h,

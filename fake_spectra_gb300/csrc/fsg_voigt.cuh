@@ -180,6 +180,57 @@ __device__ __forceinline__ void stage_voigt32(float2 *tab)
     }
 }
 
+// Wing form, valid for |u| >= 6.5 where exp(a^2 - x^2) < 1e-18 is negligible:
+// branch-free, so several nodes interleave.
+__device__ __forceinline__ float voigt_wing32(float u, const Voigt32 &c)
+{
+    const float t = __fdividef(1.0f, u * u);
+    float p = 15836.1328125f;
+    p = fmaf(p, t, 2111.484375f);
+    p = fmaf(p, t, 324.84375f);
+    p = fmaf(p, t, 59.0625f);
+    p = fmaf(p, t, 13.125f);
+    p = fmaf(p, t, 3.75f);
+    p = fmaf(p, t, 1.5f);
+    p = fmaf(p, t, 1.0f);
+    float q = 1082.8125f;
+    q = fmaf(q, t, 157.5f);
+    q = fmaf(q, t, 26.25f);
+    q = fmaf(q, t, 5.0f);
+    q = fmaf(q, t, 1.0f);
+    return c.a_sqpi * t * fmaf(-c.a2 * t, q, p);
+}
+
+// Core form, valid for |u| < 6.
+__device__ __forceinline__ float voigt_core32(float u, const Voigt32 &c, const float2 *tab)
+{
+    const float x = fabsf(u);
+    const int j = __float2int_rn(x * 10.0f);
+    const float2 fg = tab[j];
+    const float x0 = (float)j * 0.1f;
+    const float d = x - x0;
+    const float m2x = -2.0f * x0;
+    const float f0 = fg.x, f1 = fg.y;
+    const float f2 = fmaf(m2x, f1, -2.0f * f0);
+    const float f3 = fmaf(m2x, f2, -4.0f * f1);
+    const float f4 = fmaf(m2x, f3, -6.0f * f2);
+    const float f5 = fmaf(m2x, f4, -8.0f * f3);
+    const float f6 = fmaf(m2x, f5, -10.0f * f4);
+    const float f7 = fmaf(m2x, f6, -12.0f * f5);
+    float g = f7 * (1.0f / 720.0f);
+    g = fmaf(g, d, f6 * (1.0f / 120.0f));
+    g = fmaf(g, d, f5 * (1.0f / 24.0f));
+    g = fmaf(g, d, f4 * (1.0f / 6.0f));
+    g = fmaf(g, d, f3 * 0.5f);
+    g = fmaf(g, d, f2);
+    g = fmaf(g, d, f1);
+    const float f3x = fmaf(fmaf(fmaf(f6 * (1.0f / 6.0f), d, f5 * 0.5f), d, f4), d, f3);
+    const float f5x = fmaf(f6, d, f5);
+    const float br = fmaf(c.c5, f5x, fmaf(-c.c3, f3x, g));
+    const float gauss = __expf(fmaf(-x, x, c.a2)) * __cosf(2.0f * x * c.a);
+    return fmaf(-c.two_a_sqpi, br, gauss);
+}
+
 template <bool COUNT>
 __device__ __forceinline__ float voigt_f32(float u, const Voigt32 &c, const float2 *tab,
                                            unsigned &n_near)
