@@ -75,6 +75,7 @@ struct fsg_context {
     DevBuf key, second, axis, pack, cell_start[3], cell_line[3];   // sightline tables
     DevBuf line_count, cursor, off, part, dr2, line_order;   // pair lists
     DevBuf ticket, bad, nbad, err, gacc, counters;           // deposit bookkeeping
+    DevBuf skey, sperm, shist, sstart, ssums;                // particle ordering
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // host mirrors
     std::vector<long long> h_off;
@@ -105,7 +106,8 @@ struct fsg_context {
         DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis, &pack,
                           &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
                           &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
-                          &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters};
+                          &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
+                          &skey, &sperm, &shist, &sstart, &ssums};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -226,9 +228,23 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
 {
     cudaStream_t s = c->stream;
     cuda_check(cudaEventRecord(c->ev[0], s), "event");
+    // spatial order of the particles (counting sort by 3-D cell)
+    int *perm = nullptr;
+    if (p.n > 0) {
+        const int G = sort_grid_side(p.n);
+        const size_t M = (size_t)G * G * G;
+        auto *key = (unsigned *)c->ensure(c->skey, sizeof(unsigned) * p.n);
+        perm = (int *)c->ensure(c->sperm, sizeof(int) * p.n);
+        auto *hist = (unsigned *)c->ensure(c->shist, sizeof(unsigned) * M);
+        auto *start = (unsigned *)c->ensure(c->sstart, sizeof(unsigned) * M);
+        auto *sums = (unsigned *)c->ensure(c->ssums, sizeof(unsigned) * (M / 2048 + 2));
+        launch_particle_order(p, c->tables.box, G, key, hist, start, sums, perm, s);
+        c->stats.gpu_launches += 5;
+        cuda_check(cudaGetLastError(), "particle order launch");
+    }
     auto *cnt = (unsigned long long *)c->ensure(c->line_count, sizeof(unsigned long long) * nlos);
     cuda_check(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * nlos, s), "memset");
-    launch_count_pairs(c->tables, p, cnt, nullptr, s);
+    launch_count_pairs(c->tables, p, perm, cnt, nullptr, s);
     if (p.n > 0)
         c->stats.gpu_launches++;
     cuda_check(cudaGetLastError(), "count_pairs launch");
@@ -251,7 +267,7 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
     cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
     if (total > 0) {
-        launch_emit_pairs(c->tables, p, off, cur, part, dr2, err, s);
+        launch_emit_pairs(c->tables, p, perm, off, cur, part, dr2, err, s);
         c->stats.gpu_launches++;
         cuda_check(cudaGetLastError(), "emit_pairs launch");
     }

@@ -450,12 +450,13 @@ struct Tau32 {
         return total;
     }
 
-    // pixel z = zmax + koff
+    // pixel z = zmax + koff; kf == (float)koff, carried by the caller so no
+    // int->float conversion runs per pixel
     template <bool COUNT>
-    __device__ __forceinline__ float taulast(int koff, unsigned *dev_err, const float2 *tab,
+    __device__ __forceinline__ float taulast(float kf, unsigned *dev_err, const float2 *tab,
                                              Counters &ct) const
     {
-        const float k = (float)koff;
+        const float k = kf;
         const float vlow_b = fmaf(k, bintov, base0) * inv_b;   // (v_low - v_particle) / b
         if (npoints == 1)
             return scale * inner<COUNT>(vlow_b + hbin_b, tab, ct);
@@ -676,8 +677,12 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
     const int half = nbins / 2;
     const R tautail = (R)a.lp.tautail;
     const int j0 = wrap_bin(s.zmax, nbins);
+    const float lane_f = (float)lane;
     for (int dir = 0; dir < 2; dir++) {
-        for (int step = 0; step < half; step += 32) {
+        // kf tracks (float)koff exactly (integers below 2^24) without conversions
+        float kf = dir == 0 ? lane_f : -1.0f - lane_f;
+        const float dkf = dir == 0 ? 32.0f : -32.0f;
+        for (int step = 0; step < half; step += 32, kf += dkf) {
             const int k = step + lane;
             const bool valid = k < half;
             const int koff = dir == 0 ? k : -1 - k;
@@ -688,7 +693,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
                     tl = s.template taulast<COUNT>(koff, a.dev_err, c1);
             } else {
                 // every lane evaluates (warp-uniform fast paths vote inside)
-                tl = s.template taulast<COUNT>(koff, a.dev_err, tab, c1);
+                tl = s.template taulast<COUNT>(kf, a.dev_err, tab, c1);
             }
             const bool stop = valid && (tl < tautail);
             const unsigned m = __ballot_sync(0xffffffffu, stop);

@@ -17,7 +17,11 @@
 // every dr2 bit equal the reference's.  Degenerate smoothing lengths are
 // resolved exactly (see for_each_pair).
 //
-// Two passes: count (per-sightline totals) and emit (atomic slot per pair).
+// Particles are first ordered by a 3-D spatial cell (counting sort), so that
+// the 32 lanes of a warp are neighbours: they read the same cells and
+// sightlines (broadcast loads, L1 hits) and share atomics on the same
+// sightline counters.  Two passes: count (per-sightline totals) and emit (one
+// slot per pair, consecutive within a warp's group).
 #include "fsg_internal.cuh"
 
 namespace fsg {
@@ -223,16 +227,32 @@ __device__ __forceinline__ void for_each_pair(const LineTables &t, const float *
     }
 }
 
-__global__ void count_pairs_kernel(LineTables t, Particles p, unsigned long long *line_count,
-                                   unsigned char *part_flag)
+__device__ __forceinline__ void load_particle(const Particles &p, long long i, float *pos3,
+                                              float *hh)
+{
+    pos3[0] = __ldg(&p.pos[3 * i]);
+    pos3[1] = __ldg(&p.pos[3 * i + 1]);
+    pos3[2] = __ldg(&p.pos[3 * i + 2]);
+    *hh = __ldg(&p.hh[i]);
+}
+
+// Lanes that meet the same sightline together share one atomic (the particles
+// of a warp are spatial neighbours once sorted, so they often do).
+__global__ void count_pairs_kernel(LineTables t, Particles p, const int *perm,
+                                   unsigned long long *line_count, unsigned char *part_flag)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
-        float pos3[3] = {p.pos[3 * i], p.pos[3 * i + 1], p.pos[3 * i + 2]};
-        const float hh = p.hh[i];
+    const int lane = threadIdx.x & 31;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < p.n; k += stride) {
+        const long long i = perm ? (long long)perm[k] : k;
+        float pos3[3], hh;
+        load_particle(p, i, pos3, &hh);
         int found = 0;
         for_each_pair(t, pos3, hh, [&](int l, double) {
-            atomicAdd(&line_count[l], 1ull);
+            const unsigned am = __activemask();
+            const unsigned g = __match_any_sync(am, l);
+            if (lane == __ffs(g) - 1)
+                atomicAdd(&line_count[l], (unsigned long long)__popc(g));
             found = 1;
         });
         if (part_flag)
@@ -240,16 +260,26 @@ __global__ void count_pairs_kernel(LineTables t, Particles p, unsigned long long
     }
 }
 
-__global__ void emit_pairs_kernel(LineTables t, Particles p, const long long *off,
+__global__ void emit_pairs_kernel(LineTables t, Particles p, const int *perm, const long long *off,
                                   unsigned long long *cursor, int *part, double *dr2,
                                   unsigned *dev_err)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
-        float pos3[3] = {p.pos[3 * i], p.pos[3 * i + 1], p.pos[3 * i + 2]};
-        const float hh = p.hh[i];
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < p.n; k += stride) {
+        const long long i = perm ? (long long)perm[k] : k;
+        float pos3[3], hh;
+        load_particle(p, i, pos3, &hh);
         for_each_pair(t, pos3, hh, [&](int l, double d) {
-            const long long slot = off[l] + (long long)atomicAdd(&cursor[l], 1ull);
+            const unsigned am = __activemask();
+            const unsigned g = __match_any_sync(am, l);
+            const int leader = __ffs(g) - 1;
+            unsigned long long base = 0;
+            if (lane == leader)
+                base = atomicAdd(&cursor[l], (unsigned long long)__popc(g));
+            base = __shfl_sync(g, base, leader);
+            const long long slot = off[l] + (long long)base + __popc(g & below);
             if (slot < off[l + 1]) {
                 part[slot] = (int)i;
                 dr2[slot] = d;
@@ -257,6 +287,100 @@ __global__ void emit_pairs_kernel(LineTables t, Particles p, const long long *of
                 atomicOr(dev_err, (unsigned)DEVERR_PAIR_SLOT);
             }
         });
+    }
+}
+
+// ------------------------------------------------------ particle ordering
+__global__ void cell_hist_kernel(Particles p, float scale, int G, unsigned *key, unsigned *hist)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const float gmax = (float)(G - 1);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += stride) {
+        // fmaxf/fminf map NaN to 0 and clamp out-of-box positions to the edge cells
+        const float fx = fminf(fmaxf(floorf(__ldg(&p.pos[3 * i]) * scale), 0.f), gmax);
+        const float fy = fminf(fmaxf(floorf(__ldg(&p.pos[3 * i + 1]) * scale), 0.f), gmax);
+        const float fz = fminf(fmaxf(floorf(__ldg(&p.pos[3 * i + 2]) * scale), 0.f), gmax);
+        const unsigned c = ((unsigned)fx * G + (unsigned)fy) * G + (unsigned)fz;
+        key[i] = c;
+        atomicAdd(&hist[c], 1u);
+    }
+}
+
+// Exclusive scan, three kernels: per-1024-thread block (2048 elements) scans
+// with block totals, a single-block scan of the totals, and the offsets added back.
+constexpr int SCAN_T = 1024, SCAN_E = 2 * SCAN_T;
+
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned *buf)
+{
+    // Blelloch scan of SCAN_E elements in shared memory; returns the total
+    const int t = threadIdx.x;
+    int off = 1;
+    for (int d = SCAN_E >> 1; d > 0; d >>= 1) {
+        __syncthreads();
+        if (t < d) {
+            const int ai = off * (2 * t + 1) - 1, bi = off * (2 * t + 2) - 1;
+            buf[bi] += buf[ai];
+        }
+        off <<= 1;
+    }
+    __syncthreads();
+    const unsigned total = buf[SCAN_E - 1];
+    __syncthreads();
+    if (t == 0)
+        buf[SCAN_E - 1] = 0;
+    for (int d = 1; d < SCAN_E; d <<= 1) {
+        off >>= 1;
+        __syncthreads();
+        if (t < d) {
+            const int ai = off * (2 * t + 1) - 1, bi = off * (2 * t + 2) - 1;
+            const unsigned v = buf[ai];
+            buf[ai] = buf[bi];
+            buf[bi] += v;
+        }
+    }
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(SCAN_T) scan_blocks_kernel(const unsigned *in, unsigned *out,
+                                                            unsigned *sums, int n)
+{
+    __shared__ unsigned buf[SCAN_E];
+    const int base = blockIdx.x * SCAN_E;
+    for (int k = threadIdx.x; k < SCAN_E; k += SCAN_T)
+        buf[k] = (base + k < n) ? in[base + k] : 0u;
+    const unsigned total = block_exclusive_scan(buf);
+    for (int k = threadIdx.x; k < SCAN_E; k += SCAN_T)
+        if (base + k < n)
+            out[base + k] = buf[k];
+    if (threadIdx.x == 0)
+        sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_T) scan_sums_kernel(unsigned *sums, int nb)
+{
+    // nb <= SCAN_E (G <= 128)
+    __shared__ unsigned buf[SCAN_E];
+    for (int k = threadIdx.x; k < SCAN_E; k += SCAN_T)
+        buf[k] = (k < nb) ? sums[k] : 0u;
+    block_exclusive_scan(buf);
+    for (int k = threadIdx.x; k < nb; k += SCAN_T)
+        sums[k] = buf[k];
+}
+
+__global__ void add_sums_kernel(unsigned *out, const unsigned *sums, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n)
+        out[k] += sums[k / SCAN_E];
+}
+
+__global__ void cell_scatter_kernel(const unsigned *key, unsigned *cursor, int *perm, long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned slot = atomicAdd(&cursor[key[i]], 1u);
+        perm[slot] = (int)i;
     }
 }
 
@@ -274,21 +398,45 @@ int search_grid(long long n)
 
 }  // namespace
 
-void launch_count_pairs(const LineTables &t, const Particles &p, unsigned long long *line_count,
-                        unsigned char *part_flag, cudaStream_t s)
+void launch_count_pairs(const LineTables &t, const Particles &p, const int *perm,
+                        unsigned long long *line_count, unsigned char *part_flag, cudaStream_t s)
 {
     if (p.n == 0)
         return;
-    count_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, line_count, part_flag);
+    count_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, line_count, part_flag);
 }
 
-void launch_emit_pairs(const LineTables &t, const Particles &p, const long long *off,
-                       unsigned long long *cursor, int *part, double *dr2, unsigned *dev_err,
-                       cudaStream_t s)
+void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
+                       const long long *off, unsigned long long *cursor, int *part, double *dr2,
+                       unsigned *dev_err, cudaStream_t s)
 {
     if (p.n == 0)
         return;
-    emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, off, cursor, part, dr2, dev_err);
+    emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, off, cursor, part, dr2,
+                                                       dev_err);
+}
+
+// ~64 particles per cell, at most 128^3 cells (the totals then fit one scan block)
+int sort_grid_side(long long n)
+{
+    int G = (int)cbrt((double)n / 64.0);
+    return G < 1 ? 1 : (G > 128 ? 128 : G);
+}
+
+void launch_particle_order(const Particles &p, double box, int G, unsigned *key, unsigned *hist,
+                           unsigned *start, unsigned *sums, int *perm, cudaStream_t s)
+{
+    if (p.n == 0)
+        return;
+    const int M = G * G * G;
+    cudaMemsetAsync(hist, 0, sizeof(unsigned) * M, s);
+    cell_hist_kernel<<<search_grid(p.n), 256, 0, s>>>(p, (float)(G / box), G, key, hist);
+    const int nb = (M + SCAN_E - 1) / SCAN_E;
+    scan_blocks_kernel<<<nb, SCAN_T, 0, s>>>(hist, start, sums, M);
+    scan_sums_kernel<<<1, SCAN_T, 0, s>>>(sums, nb);
+    add_sums_kernel<<<(M + 255) / 256, 256, 0, s>>>(start, sums, M);
+    // the scan output is consumed as the scatter cursor
+    cell_scatter_kernel<<<search_grid(p.n), 256, 0, s>>>(key, start, perm, p.n);
 }
 
 }  // namespace fsg

@@ -111,11 +111,19 @@ struct PairLists {
 };
 
 // Host launchers (stream-ordered; no synchronisation inside).
-void launch_count_pairs(const LineTables &t, const Particles &p, unsigned long long *line_count,
-                        unsigned char *part_flag, cudaStream_t s);
-void launch_emit_pairs(const LineTables &t, const Particles &p, const long long *off,
-                       unsigned long long *cursor, int *part, double *dr2, unsigned *dev_err,
-                       cudaStream_t s);
+// perm (may be null = identity): the order in which particles are visited.
+void launch_count_pairs(const LineTables &t, const Particles &p, const int *perm,
+                        unsigned long long *line_count, unsigned char *part_flag, cudaStream_t s);
+void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
+                       const long long *off, unsigned long long *cursor, int *part, double *dr2,
+                       unsigned *dev_err, cudaStream_t s);
+
+// Counting sort of the particles by a G^3 spatial cell, so that the search
+// visits neighbouring particles together.  Scratch: key[N], perm[N] (output),
+// hist[G^3], start[G^3], sums[G^3/2048 + 1].
+int sort_grid_side(long long n);
+void launch_particle_order(const Particles &p, double box, int G, unsigned *key, unsigned *hist,
+                           unsigned *start, unsigned *sums, int *perm, cudaStream_t s);
 
 struct DepositLaunch {
     int precision;           // 0 = FP64 plain, 1 = FP32 tuned

@@ -262,7 +262,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     Particles p{pos, compute_tau ? vel : nullptr, dens, compute_tau ? temp : nullptr, h,
                 (long long)npart};
     NA_CUDA(cudaMemsetAsync(d_count, 0, 8ull * nlos, s), "memset");
-    launch_count_pairs(t, p, d_count, nullptr, s);
+    launch_count_pairs(t, p, nullptr, d_count, nullptr, s);
     NA_CUDA(cudaGetLastError(), "count_pairs launch");
     NA_CUDA(cudaMemcpyAsync(h_count, d_count, 8ull * nlos, cudaMemcpyDeviceToHost, s),
             "read counts");
@@ -280,7 +280,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     NA_CUDA(cudaMemsetAsync(d_cursor, 0, 8ull * nlos, s), "memset");
     NA_CUDA(cudaMemsetAsync(d_err, 0, 4, s), "memset");
     if (total > 0) {
-        launch_emit_pairs(t, p, d_off, d_cursor, d_part, d_dr2, d_err, s);
+        launch_emit_pairs(t, p, nullptr, d_off, d_cursor, d_part, d_dr2, d_err, s);
         NA_CUDA(cudaGetLastError(), "emit_pairs launch");
     }
     for (int i = 0; i < nlos; i++)

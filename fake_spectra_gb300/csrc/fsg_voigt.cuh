@@ -202,12 +202,22 @@ __device__ __forceinline__ float voigt_wing32(float u, const Voigt32 &c)
 }
 
 // Core form, valid for |u| < 6.
+// Nearest table index of x >= 0 (x < 6) without int<->float conversions, which
+// run on the narrow FP64/conversion pipe of this GPU: adding 1.5 * 2^23 rounds
+// x*10 to an integer held in the low mantissa bits.
+__device__ __forceinline__ int vtab_index(float x, float &x0)
+{
+    const float m = fmaf(x, 10.0f, 12582912.0f);
+    x0 = (m - 12582912.0f) * 0.1f;
+    return __float_as_int(m) - 0x4B400000;
+}
+
 __device__ __forceinline__ float voigt_core32(float u, const Voigt32 &c, const float2 *tab)
 {
     const float x = fabsf(u);
-    const int j = __float2int_rn(x * 10.0f);
+    float x0;
+    const int j = vtab_index(x, x0);
     const float2 fg = tab[j];
-    const float x0 = (float)j * 0.1f;
     const float d = x - x0;
     const float m2x = -2.0f * x0;
     const float f0 = fg.x, f1 = fg.y;
@@ -239,9 +249,9 @@ __device__ __forceinline__ float voigt_f32(float u, const Voigt32 &c, const floa
     if (x < 6.0f) {
         if (COUNT)
             n_near++;
-        const int j = __float2int_rn(x * 10.0f);
+        float x0;
+        const int j = vtab_index(x, x0);
         const float2 fg = tab[j];
-        const float x0 = (float)j * 0.1f;
         const float d = x - x0;
         const float m2x = -2.0f * x0;
         const float f0 = fg.x, f1 = fg.y;
