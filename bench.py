@@ -62,6 +62,8 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-bwd", action="store_true")
     return p.parse_args()
 
 
@@ -335,6 +337,82 @@ def main():
                            "tau_rel_err_median": float(np.median(rel)),
                            "colden_rel_err_max": float(crel.max()),
                            "against": "plain FP64 form on the same %d sightlines" % len(lines)}
+
+    # ---- batched form: every line of the workload (tau) plus the column densities, one call
+    if not args.no_batch and len(w.transitions) > 1:
+        blines = [(t, w.dens[t.species], True, t.name != "lyb") for t in w.transitions]
+
+        def batch():
+            return interp.spectra_batch_device(ctx, w.nbins, w.kernel, w.box, w.velfac, w.atime,
+                                               w.tautail, w.pos, w.vel, w.temp, w.hh, w.axis,
+                                               w.cofm, blines, precision="fp32")
+        outs = batch()
+        del outs
+        torch.cuda.synchronize()
+        nb = max(1, min(args.steps, 2))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(nb):
+            outs = batch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        msb = e0.elapsed_time(e1) / nb
+        ntau = sum(1 for b in blines if b[2])
+        ncol = sum(1 for b in blines if b[3])
+        res["batched"] = {"ms_per_call": msb, "lines": [t.name for t in w.transitions],
+                          "tau_arrays": ntau, "colden_arrays": ncol,
+                          "tau_pixels_per_s": ntau * pixels / (msb * 1e-3),
+                          "graph": "one CUDA graph of all deposits after one sightline search"}
+        del outs
+
+    # ---- differentiation form: forward and forward+backward on the 128^3 workload
+    if not args.no_bwd:
+        from fake_spectra_gb300.autograd import particle_tau
+        w4 = synth.generate_torch(4, device="cuda")
+        w4t = synth.generate_torch(4, seed=5, device="cuda")
+        t4 = synth.LYA
+        a4 = lambda wk: (wk.nbins, wk.kernel, wk.box, wk.velfac, wk.atime, t4.lambda_cm,
+                         t4.gamma, t4.fosc, t4.amumass, wk.tautail)
+        ftarget = torch.exp(-interp.particle_interpolate_device(
+            ctx, *w4t.call_args(t4, 1)[:11], w4t.pos, w4t.vel, w4t.dens["HI"], w4t.temp,
+            w4t.hh, w4t.axis, w4t.cofm, precision="fp32"))
+        dens4 = w4.dens["HI"].clone().requires_grad_(True)
+        temp4 = w4.temp.clone().requires_grad_(True)
+        vel4 = w4.vel.clone().requires_grad_(True)
+
+        def fwd():
+            return particle_tau(ctx, *a4(w4), w4.pos, vel4, dens4, temp4, w4.hh, w4.axis,
+                                w4.cofm)
+
+        def fwd_bwd():
+            tau = fwd()
+            loss = ((torch.exp(-tau) - ftarget) ** 2).sum()
+            loss.backward()
+            return loss
+
+        for _ in range(2):
+            fwd_bwd()
+        nr = max(3, args.steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.no_grad():
+            e0.record(stream)
+            for _ in range(nr):
+                fwd()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        msf = e0.elapsed_time(e1) / nr
+        e0.record(stream)
+        for _ in range(nr):
+            fwd_bwd()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        msfb = e0.elapsed_time(e1) / nr
+        res["fwd_bwd"] = {"workload": w4.name, "particles": w4.npart, "sightlines": w4.nlos,
+                          "nbins": w4.nbins, "fwd_ms": msf, "fwd_bwd_ms": msfb,
+                          "ratio": msfb / msf,
+                          "loss": "sum (exp(-tau) - F_target)^2, F_target from seed 5",
+                          "grads": "dens, temp, v_los (FP32 backward kernel)"}
+        del w4, w4t, dens4, temp4, vel4, ftarget
 
     # ---- end to end through the host-pointer C ABI (copies inside the timed region)
     if not args.no_e2e:

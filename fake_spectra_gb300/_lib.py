@@ -31,6 +31,8 @@ EXPORTS = (
     "fsg_context_stats",
     "fsg_particle_interpolate",
     "fsg_particle_interpolate_device",
+    "fsg_spectra_batch_device",
+    "fsg_tau_backward_device",
     "fsg_build_pairs_device",
     "fsg_copy_pairs",
     "fsg_particle_interpolate_noalloc",
@@ -54,6 +56,11 @@ class Stats(ctypes.Structure):
                 ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d),
                 ("evals_core", _c_i64), ("evals_wing", _c_i64), ("evals_other", _c_i64),
                 ("pixels", _c_i64)]
+
+
+class Line(ctypes.Structure):
+    _fields_ = [("lambda_", _c_d), ("gamma", _c_d), ("fosc", _c_d), ("amumass", _c_d),
+                ("dens", _p), ("tau", _p), ("colden", _p)]
 
 
 class FsgError(RuntimeError):
@@ -109,6 +116,12 @@ def load(path=None):
         L.fsg_context_stats.argtypes = [_p, ctypes.POINTER(Stats)]
         L.fsg_particle_interpolate.argtypes = _INTERP_ARGS
         L.fsg_particle_interpolate_device.argtypes = [_p] + _INTERP_ARGS
+        L.fsg_spectra_batch_device.argtypes = ([_p, _c_int, _c_int] + [_c_d] * 4 + [_p] * 4 +
+                                               [_c_i64, _p, _p, _c_i32, _c_int,
+                                                ctypes.POINTER(Line), _p, _p, _c_size])
+        L.fsg_tau_backward_device.argtypes = ([_p, _c_int, _c_int] + [_c_d] * 8 + [_p] * 5 +
+                                              [_c_i64, _p, _p, _c_i32, _p, _p, _p, _p, _p,
+                                               _c_size])
         L.fsg_build_pairs_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32,
                                              ctypes.POINTER(_c_i64), _p, _c_size]
         L.fsg_copy_pairs.argtypes = [_p, _p, _p, _p, _c_int, _p, _c_size]

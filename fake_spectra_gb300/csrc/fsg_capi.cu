@@ -80,6 +80,9 @@ struct fsg_context {
     // host mirrors
     std::vector<long long> h_off;
     std::vector<int> h_order;
+    // batched form: instantiated graph of the deposits and the call it was built for
+    cudaGraphExec_t graph = nullptr;
+    std::vector<double> graph_key;
     int nlos = 0;
     long long npairs = 0;
     LineTables tables{};
@@ -397,6 +400,123 @@ LineParams make_line_params(int compute_tau, int nbins, int kernel, double box, 
     return lp;
 }
 
+// Launch configuration of the deposit for this call.
+DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt)
+{
+    DepositLaunch cfg{};
+    cfg.precision = opt ? opt->precision : FSG_PREC_FP64;
+    if (cfg.precision != FSG_PREC_FP64 && cfg.precision != FSG_PREC_FP32)
+        fail(FSG_ERR_VALUE, "unknown precision %d", cfg.precision);
+    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
+    cfg.threads = (opt && opt->threads > 0) ? opt->threads : tmax;
+    if (cfg.threads % 32 || cfg.threads > tmax)
+        fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
+    cfg.smem_mode = lp.nbins <= deposit_max_smem_bins();
+    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent
+                                                    : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    const int per_sm = std::max(1, deposit_resident_ctas(lp.compute_tau, cfg.precision,
+                                                         cfg.threads, lp.nbins, cfg.smem_mode));
+    cfg.grid = std::min(c->nlos, sms * per_sm);
+    return cfg;
+}
+
+// The batched form (fsg_spectra_batch_device): every deposit of the call in
+// one CUDA graph, re-captured only when the call's shape or buffers change.
+void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
+               const std::vector<const float *> &dens, const std::vector<double *> &outs,
+               const Particles &p0, const fsg_options *opt)
+{
+    const int nlos = c->nlos;
+    const int nb = lps.empty() ? 0 : lps[0].nbins;
+    const size_t nout = (size_t)nlos * nb;
+    if (nout == 0 || lps.empty())
+        return;
+    PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
+    std::vector<DepositLaunch> cfgs;
+    for (const LineParams &lp : lps)
+        cfgs.push_back(deposit_config(c, lp, opt));
+    unsigned long long *gacc = nullptr;
+    if (!cfgs[0].smem_mode)
+        gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
+    auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
+    auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
+    auto *nbad = (int *)c->ensure(c->nbad, sizeof(int));
+    auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
+    // graph key: everything the captured launches depend on
+    std::vector<double> key;
+    auto put = [&](double v) { key.push_back(v); };
+    auto putp = [&](const void *q) { key.push_back((double)(uintptr_t)q); };
+    put(nlos);
+    put(c->npairs);
+    putp(c->off.p);
+    putp(c->part.p);
+    putp(c->dr2.p);
+    putp(c->line_order.p);
+    putp(c->key.p);
+    putp(c->second.p);
+    putp(c->axis.p);
+    putp(c->pack.p);
+    putp(gacc);
+    putp(p0.pos);
+    putp(p0.vel);
+    putp(p0.temp);
+    putp(p0.hh);
+    put((double)p0.n);
+    for (size_t k = 0; k < lps.size(); k++) {
+        const LineParams &lp = lps[k];
+        for (double v : {(double)lp.compute_tau, (double)lp.nbins, (double)lp.kernel, lp.tautail,
+                         lp.sigma_a, lp.bfac, lp.voigt_fac, lp.velfac, lp.vbox, lp.box})
+            put(v);
+        putp(dens[k]);
+        putp(outs[k]);
+        put(cfgs[k].precision);
+        put(cfgs[k].threads);
+        put(cfgs[k].persistent);
+        put(cfgs[k].grid);
+    }
+    cudaStream_t s = c->own;
+    cuda_check(cudaStreamSynchronize(c->stream), "sync caller stream");
+    if (!c->graph || key != c->graph_key) {
+        if (c->graph) {
+            cudaGraphExecDestroy(c->graph);
+            c->graph = nullptr;
+        }
+        cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "begin capture");
+        cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+        for (size_t k = 0; k < lps.size(); k++) {
+            Particles p = p0;
+            p.dens = dens[k];
+            cudaMemsetAsync(outs[k], 0, sizeof(double) * nout, s);
+            cudaMemsetAsync(ticket, 0, sizeof(unsigned), s);
+            cudaMemsetAsync(nbad, 0, sizeof(int), s);
+            launch_deposit(lps[k], c->tables, p, pl, (const int *)c->line_order.p, nlos, outs[k],
+                           ticket, bad, nbad, err, gacc, nullptr, cfgs[k], s);
+            launch_deposit_fallback_dev(lps[k], c->tables, p, pl, bad, nbad, nlos, outs[k], err,
+                                        s);
+        }
+        cudaGraph_t g = nullptr;
+        cuda_check(cudaStreamEndCapture(s, &g), "end capture");
+        cudaError_t e = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(e, "graph instantiate");
+        c->graph_key = key;
+    }
+    cuda_check(cudaEventRecord(c->ev[2], s), "event");
+    cuda_check(cudaGraphLaunch(c->graph, s), "graph launch");
+    c->stats.gpu_launches += 2 * (int64_t)lps.size();
+    cuda_check(cudaEventRecord(c->ev[3], s), "event");
+    unsigned h_err = 0;
+    cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "batch");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    c->stats.ms_deposit = ms;
+    if (h_err)
+        fail(FSG_ERR_DEVICE, "deposit kernels reported device error bits 0x%x", h_err);
+}
+
 fsg_context *g_default[64] = {nullptr};
 std::mutex g_default_mu;
 
@@ -478,6 +598,8 @@ void fsg_context_destroy(fsg_context *ctx)
     for (auto &e : ctx->ev)
         if (e)
             cudaEventDestroy(e);
+    if (ctx->graph)
+        cudaGraphExecDestroy(ctx->graph);
     if (ctx->own)
         cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -571,6 +693,111 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         if (nout)
             cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "D2H");
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_spectra_batch_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
+                             double atime, double tautail, const float *pos, const float *vel,
+                             const float *temp, const float *h, int64_t npart,
+                             const int32_t *axis, const double *cofm, int32_t nlos, int nlines,
+                             const fsg_line *lines, const fsg_options *opt, char *errbuf,
+                             size_t errlen)
+{
+    (void)atime;
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        if (nlines < 0 || (nlines > 0 && !lines))
+            fail(FSG_ERR_VALUE, "bad line list");
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        bool any_tau = false;
+        for (int k = 0; k < nlines; k++) {
+            if (!lines[k].dens)
+                fail(FSG_ERR_VALUE, "line %d has no density array", k);
+            any_tau |= lines[k].tau != nullptr;
+        }
+        if (any_tau && (!vel || !temp))
+            fail(FSG_ERR_VALUE, "tau needs vel and temp");
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        build_tables(ctx, axis, cofm, nlos, box);
+        Particles p{pos, vel, nullptr, temp, h, (long long)npart};
+        search_pairs(ctx, p, nlos);
+        std::vector<LineParams> lps;
+        std::vector<const float *> dens;
+        std::vector<double *> outs;
+        for (int k = 0; k < nlines; k++) {
+            const fsg_line &L = lines[k];
+            if (L.tau) {
+                lps.push_back(make_line_params(1, nbins, kernel, box, velfac, L.lambda, L.gamma,
+                                               L.fosc, L.amumass, tautail));
+                dens.push_back(L.dens);
+                outs.push_back(L.tau);
+            }
+            if (L.colden) {
+                lps.push_back(make_line_params(0, nbins, kernel, box, velfac, L.lambda, L.gamma,
+                                               L.fosc, L.amumass, tautail));
+                dens.push_back(L.dens);
+                outs.push_back(L.colden);
+            }
+        }
+        run_batch(ctx, lps, dens, outs, p, opt);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
+                            double atime, double lambda, double gamma, double fosc,
+                            double amumass, double tautail, const float *pos, const float *vel,
+                            const float *dens, const float *temp, const float *h, int64_t npart,
+                            const int32_t *axis, const double *cofm, int32_t nlos,
+                            const double *grad_tau, float *grad_dens, float *grad_temp,
+                            float *grad_vel, char *errbuf, size_t errlen)
+{
+    (void)atime;
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        if (!grad_tau || !grad_dens || !grad_temp || !grad_vel)
+            fail(FSG_ERR_VALUE, "gradient buffers must not be NULL");
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        build_tables(ctx, axis, cofm, nlos, box);
+        Particles p{pos, vel, dens, temp, h, (long long)npart};
+        search_pairs(ctx, p, nlos);
+        if (nlos == 0 || nbins == 0 || ctx->npairs == 0)
+            return FSG_OK;
+        LineParams lp = make_line_params(1, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                                         amumass, tautail);
+        PairLists pl{(const long long *)ctx->off.p, (const int *)ctx->part.p,
+                     (const double *)ctx->dr2.p};
+        cudaStream_t s = ctx->stream;
+        auto *ticket = (unsigned *)ctx->ensure(ctx->ticket, sizeof(unsigned));
+        auto *err = (unsigned *)ctx->ensure(ctx->err, sizeof(unsigned));
+        cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
+        cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int grid = std::min(nlos, sms * std::max(1, tau_backward_resident_ctas()));
+        cuda_check(cudaEventRecord(ctx->ev[2], s), "event");
+        launch_tau_backward(lp, ctx->tables, p, pl, (const int *)ctx->line_order.p, nlos,
+                            grad_tau, grad_dens, grad_temp, grad_vel, ticket, err, grid, s);
+        ctx->stats.gpu_launches++;
+        cuda_check(cudaGetLastError(), "backward launch");
+        cuda_check(cudaEventRecord(ctx->ev[3], s), "event");
+        unsigned h_err = 0;
+        cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s),
+                   "read");
+        cuda_check(cudaStreamSynchronize(s), "backward");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+        ctx->stats.ms_deposit = ms;
+        if (h_err)
+            fail(FSG_ERR_DEVICE, "backward kernel reported device error bits 0x%x", h_err);
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);

@@ -345,7 +345,7 @@ __device__ __noinline__ float voigt_wide32(float u, double a)
 struct Tau32 {
     Voigt32 vc;
     float U[NODES], w[NODES];   // node velocities / b and kernel weights
-    float inv_b, base0, bintov, hbin_b, scale, sub_dv;
+    float inv_b, base0, bintov, hbin_b, scale, scale_nod, sub_dv;
     float aa_f;
     double aa_d;
     long long zmax;
@@ -392,10 +392,11 @@ struct Tau32 {
         // Float node offsets U_i = v_i / b keep ~1e-5 absolute accuracy only while
         // |U_i| <= 256; sub-sampled or very narrow profiles take the FP64 walk.
         careful = wide || npoints > 8 || (double)vhigh > 256.0 * btherm;
-        double sc = amp * (double)in.dens / lp.velfac * (double)deltav;
+        double sc = amp / lp.velfac * (double)deltav;
         if (npoints > 1)
             sc /= (npoints - 1);
-        scale = (float)sc;
+        scale_nod = (float)sc;
+        scale = (float)(sc * (double)in.dens);
         hbin_b = 0.5f * bintov * inv_b;
         sub_dv = npoints > 1 ? (float)(bintov_d / (npoints - 1)) * inv_b : 0.f;
         return true;
@@ -863,8 +864,12 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
 template <bool TAU>
 __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables t, Particles p,
                                                        PairLists pl, const int *bad_lines,
-                                                       double *out, unsigned *dev_err)
+                                                       const int *n_bad_dev, double *out,
+                                                       unsigned *dev_err)
 {
+    // with n_bad_dev the grid covers every sightline and the count is read here
+    if (n_bad_dev && (int)blockIdx.x >= *n_bad_dev)
+        return;
     const int line = bad_lines[blockIdx.x];
     const int axis = t.axis[line];
     const int nbins = lp.nbins;
@@ -909,6 +914,216 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
             for (long long z = c.zlow + lane; z <= c.zhigh; z += 32)
                 atomicAdd(&row[wrap_bin(z, nbins)], c.value64(z));
         }
+    }
+}
+
+// ============================================================ backward
+// dL/d(dens), dL/dT and dL/d(v_los) per particle from dL/dtau per pixel, for
+// the FP32 form.  The window of every pair is recomputed with the forward's
+// stop rule (and is treated as fixed, like the sub-sample count).  For a pair
+// with tau contribution c_j = scale * S_j, S_j = sum_i w_i H(u_ij, a):
+//   dc_j/d(dens)  = scale_nod * S_j
+//   dc_j/d(v_los) = scale / b * sum_i w_i dH/du          (du/dv = 1/b)
+//   dc_j/dT       = -scale / (2T) * sum_i w_i (H + u dH/du + a dH/da)
+// (amp ~ 1/b, u ~ 1/b, a ~ 1/b and db/dT = b/(2T)).
+struct GradArgs {
+    LineParams lp;
+    LineTables t;
+    Particles p;
+    PairLists pl;
+    const int *line_order;
+    int nlos;
+    const double *grad_tau;
+    float *g_dens, *g_temp, *g_vel;
+    unsigned *ticket;
+    unsigned *dev_err;
+};
+
+struct GradSums {
+    float d, v, t;
+};
+
+__device__ __forceinline__ GradSums grad_node_sums(const Tau32 &s, float V, const float2 *tab)
+{
+    GradSums g = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < NODES; ++i) {
+        const float u = s.U[i] - V;
+        const VoigtGrad r = voigt_grad32(u, s.vc, tab);
+        g.d = fmaf(s.w[i], r.h, g.d);
+        g.v = fmaf(s.w[i], r.hu, g.v);
+        g.t = fmaf(s.w[i], r.h + fmaf(u, r.hu, s.aa_f * r.ha), g.t);
+    }
+    return g;
+}
+
+// FP64 profile and central-difference derivatives for the rare pairs that the
+// FP32 form walks in FP64 (Tau32::careful).
+__device__ __noinline__ void voigt_grad64(double u, double a, double &h, double &hu, double &ha)
+{
+    h = voigt_f64(u, a);
+    const double eu = 1e-6 * fmax(1.0, fabs(u));
+    hu = (voigt_f64(u + eu, a) - voigt_f64(u - eu, a)) / (2.0 * eu);
+    const double ea = 1e-6 * fmax(fabs(a), 1e-8);
+    ha = (voigt_f64(u, a + ea) - voigt_f64(u, a - ea)) / (2.0 * ea);
+}
+
+__device__ __noinline__ void grad_pair_careful(const GradArgs &a, const PairInput &in,
+                                               const double *gt, int lane, double &gd,
+                                               double &gv, double &gtmp)
+{
+    Tau64 s;
+    gd = gv = gtmp = 0.0;
+    if (!s.setup(a.lp, in))
+        return;
+    const int nbins = a.lp.nbins, half = nbins / 2;
+    const int j0 = wrap_bin(s.zmax, nbins);
+    const double amp_v = s.ampd / a.lp.velfac;   // amp dens / velfac
+    const double amp_nod = (s.ampd / ((double)in.dens != 0.0 ? (double)in.dens : 1.0)) /
+                           a.lp.velfac;
+    Counters ct = {0, 0, 0, 0};
+    for (int dir = 0; dir < 2; dir++) {
+        for (int step = 0; step < half; step += 32) {
+            const int k = step + lane;
+            const bool valid = k < half;
+            const int koff = dir == 0 ? k : -1 - k;
+            double tl = 0.0, sd = 0.0, sv = 0.0, stt = 0.0;
+            if (valid) {
+                tl = s.taulast<false>(koff, a.dev_err, ct);
+                const double vlow = (double)(s.zmax + koff) * s.bintov - s.vel;
+                const double vhigh = vlow + s.bintov;
+                int np = 1;
+                double dv = 0.0;
+                if (!((vhigh - vlow) < s.half_b)) {
+                    const double npd = 2 * ceil((vhigh - vlow) / s.half_b / 2) + 1.;
+                    np = npd <= MAX_SUBSAMPLES ? (int)npd : 1;
+                    dv = (vhigh - vlow) / (np - 1);
+                }
+                for (int q = 0; q < np; q++) {
+                    const double vo = np == 1 ? (vhigh + vlow) / 2. : vlow + q * dv;
+                    const double wq = (np == 1) ? 1.0 : ((q == 0 || q == np - 1) ? 0.5 : 1.0) /
+                                                           (np - 1);
+                    for (int i = 0; i < NODES; ++i) {
+                        const double u = (s.vv[i] - vo) * s.inv_b;
+                        double h, hu, ha;
+                        voigt_grad64(u, s.aa, h, hu, ha);
+                        const double ww = wq * s.w[i] * s.deltav;
+                        sd += ww * h;
+                        sv += ww * hu;
+                        stt += ww * (h + u * hu + s.aa * ha);
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, valid && tl < a.lp.tautail);
+            const int last = m ? (__ffs(m) - 1) : 31;
+            if (valid && lane <= last) {
+                const double g = gt[bin_from(j0, koff, nbins)];
+                gd += g * amp_nod * sd;
+                gv += g * amp_v * s.inv_b * sv;
+                gtmp += g * (-amp_v / (2.0 * (double)in.temp)) * stt;
+            }
+            if (m)
+                break;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(512) grad_kernel(GradArgs a)
+{
+    __shared__ float2 vtab[FSG_V32_N];
+    __shared__ unsigned s_ticket;
+    stage_voigt32(vtab);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int nbins = a.lp.nbins, half = nbins / 2;
+    const float tautail = (float)a.lp.tautail;
+    if (threadIdx.x == 0)
+        s_ticket = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    unsigned ticket = s_ticket;
+    while (ticket < (unsigned)a.nlos) {
+        const int line = a.line_order[ticket];
+        const int axis = a.t.axis[line];
+        const double *gt = a.grad_tau + (size_t)line * nbins;
+        const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
+        for (long long e = e0 + warp; e < e1; e += nwarps) {
+            const PairInput in = load_pair(a.p, a.pl, e, axis, true);
+            const int ip = a.pl.part[e];
+            Tau32 s;
+            if (!s.setup(a.lp, in))
+                continue;
+            float gd = 0.f, gv = 0.f, gtmp = 0.f;
+            if (s.careful) {
+                double d_, v_, t_;
+                grad_pair_careful(a, in, gt, lane, d_, v_, t_);
+                gd = (float)d_;
+                gv = (float)v_;
+                gtmp = (float)t_;
+            } else {
+                const int j0 = wrap_bin(s.zmax, nbins);
+                const float lane_f = (float)lane;
+                float ad = 0.f, av = 0.f, at = 0.f;
+                for (int dir = 0; dir < 2; dir++) {
+                    float kf = dir == 0 ? lane_f : -1.0f - lane_f;
+                    const float dkf = dir == 0 ? 32.0f : -32.0f;
+                    for (int step = 0; step < half; step += 32, kf += dkf) {
+                        const int k = step + lane;
+                        const bool valid = k < half;
+                        const int koff = dir == 0 ? k : -1 - k;
+                        const float vlow_b = fmaf(kf, s.bintov, s.base0) * s.inv_b;
+                        GradSums g;
+                        if (s.npoints == 1) {
+                            g = grad_node_sums(s, vlow_b + s.hbin_b, vtab);
+                        } else {
+                            g = grad_node_sums(s, vlow_b, vtab);
+                            g.d *= 0.5f;
+                            g.v *= 0.5f;
+                            g.t *= 0.5f;
+                            for (int i = 1; i < s.npoints - 1; ++i) {
+                                const GradSums h =
+                                    grad_node_sums(s, fmaf((float)i, s.sub_dv, vlow_b), vtab);
+                                g.d += h.d;
+                                g.v += h.v;
+                                g.t += h.t;
+                            }
+                            const GradSums h = grad_node_sums(s, vlow_b + 2.f * s.hbin_b, vtab);
+                            g.d += 0.5f * h.d;
+                            g.v += 0.5f * h.v;
+                            g.t += 0.5f * h.t;
+                        }
+                        const float tl = s.scale * g.d;
+                        const unsigned m = __ballot_sync(0xffffffffu, valid && tl < tautail);
+                        const int last = m ? (__ffs(m) - 1) : 31;
+                        if (valid && lane <= last) {
+                            const float gg = (float)gt[bin_from(j0, koff, nbins)];
+                            ad = fmaf(gg, g.d, ad);
+                            av = fmaf(gg, g.v, av);
+                            at = fmaf(gg, g.t, at);
+                        }
+                        if (m)
+                            break;
+                    }
+                }
+                gd = s.scale_nod * ad;
+                gv = s.scale * s.inv_b * av;
+                gtmp = -s.scale / (2.0f * in.temp) * at;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                gd += __shfl_xor_sync(0xffffffffu, gd, o);
+                gv += __shfl_xor_sync(0xffffffffu, gv, o);
+                gtmp += __shfl_xor_sync(0xffffffffu, gtmp, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&a.g_dens[ip], gd);
+                atomicAdd(&a.g_temp[ip], gtmp);
+                atomicAdd(&a.g_vel[3ll * ip + axis - 1], gv);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_ticket = atomicAdd(a.ticket, 1u);
+        __syncthreads();
+        ticket = s_ticket;
     }
 }
 
@@ -1008,9 +1223,56 @@ void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Pa
     if (n_bad <= 0)
         return;
     if (lp.compute_tau)
-        fallback_kernel<true><<<n_bad, 256, 0, s>>>(lp, t, p, pl, bad_lines, out, dev_err);
+        fallback_kernel<true><<<n_bad, 256, 0, s>>>(lp, t, p, pl, bad_lines, nullptr, out,
+                                                    dev_err);
     else
-        fallback_kernel<false><<<n_bad, 256, 0, s>>>(lp, t, p, pl, bad_lines, out, dev_err);
+        fallback_kernel<false><<<n_bad, 256, 0, s>>>(lp, t, p, pl, bad_lines, nullptr, out,
+                                                     dev_err);
+}
+
+void launch_deposit_fallback_dev(const LineParams &lp, const LineTables &t, const Particles &p,
+                                 const PairLists &pl, const int *bad_lines, const int *n_bad_dev,
+                                 int nlos, double *out, unsigned *dev_err, cudaStream_t s)
+{
+    if (nlos <= 0)
+        return;
+    if (lp.compute_tau)
+        fallback_kernel<true><<<nlos, 256, 0, s>>>(lp, t, p, pl, bad_lines, n_bad_dev, out,
+                                                   dev_err);
+    else
+        fallback_kernel<false><<<nlos, 256, 0, s>>>(lp, t, p, pl, bad_lines, n_bad_dev, out,
+                                                    dev_err);
+}
+
+void launch_tau_backward(const LineParams &lp, const LineTables &t, const Particles &p,
+                         const PairLists &pl, const int *line_order, int nlos,
+                         const double *grad_tau, float *g_dens, float *g_temp, float *g_vel,
+                         unsigned *ticket, unsigned *dev_err, int grid, cudaStream_t s)
+{
+    if (nlos == 0 || lp.nbins == 0)
+        return;
+    GradArgs a;
+    a.lp = lp;
+    a.t = t;
+    a.p = p;
+    a.pl = pl;
+    a.line_order = line_order;
+    a.nlos = nlos;
+    a.grad_tau = grad_tau;
+    a.g_dens = g_dens;
+    a.g_temp = g_temp;
+    a.g_vel = g_vel;
+    a.ticket = ticket;
+    a.dev_err = dev_err;
+    grad_kernel<<<grid, 512, 0, s>>>(a);
+}
+
+int tau_backward_resident_ctas()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, grad_kernel, 512, 0);
+    return n;
 }
 
 }  // namespace fsg
+

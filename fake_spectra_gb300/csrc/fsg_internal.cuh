@@ -150,7 +150,21 @@ void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Pa
                              const PairLists &pl, const int *bad_lines, int n_bad, double *out,
                              unsigned *dev_err, cudaStream_t s);
 
+// Same, with the count of listed sightlines read on the device (no host
+// round trip, so it can be captured in a CUDA graph): grid of nlos blocks.
+void launch_deposit_fallback_dev(const LineParams &lp, const LineTables &t, const Particles &p,
+                                 const PairLists &pl, const int *bad_lines, const int *n_bad_dev,
+                                 int nlos, double *out, unsigned *dev_err, cudaStream_t s);
+
 int deposit_max_smem_bins();
+
+// Backward of the FP32 tau deposit: accumulates (+=) dL/d(dens), dL/dT and
+// dL/d(vel[3p+axis-1]) from dL/dtau (grad_tau, [L*nbins]).  Persistent grid.
+void launch_tau_backward(const LineParams &lp, const LineTables &t, const Particles &p,
+                         const PairLists &pl, const int *line_order, int nlos,
+                         const double *grad_tau, float *g_dens, float *g_temp, float *g_vel,
+                         unsigned *ticket, unsigned *dev_err, int grid, cudaStream_t s);
+int tau_backward_resident_ctas();
 
 // Peak FMA throughput of this GPU (TFLOP/s, 2 flops per FMA), own microbenchmark.
 double measure_fma_peak(int precision, cudaStream_t s);

@@ -295,3 +295,117 @@ __device__ __forceinline__ float voigt_f32(float u, const Voigt32 &c, const floa
 }
 
 }  // namespace fsg
+
+namespace fsg {
+
+// ---------------------------------------------------------------------------
+// Voigt profile with its partial derivatives (backward pass, FP32, a <= 0.1):
+// H(u, a), dH/du and dH/da, from the same two forms as voigt_f32.
+//  wing (|u| >= 6): H = (a/sqrt(pi)) t [P(t) - a^2 t Q(t)], t = 1/u^2, so
+//    dH/du = -(a/sqrt(pi)) (t/u) [P1(t) - a^2 t Q1(t)],
+//      P1 = sum (2k+2) p_k t^k, Q1 = sum (2k+4) q_k t^k,
+//    dH/da = (1/sqrt(pi)) t [P(t) - 3 a^2 t Q(t)];
+//  core (|u| < 6): with E = exp(a^2-x^2), C = cos 2xa, S = sin 2xa,
+//    H     = E C - (2a/sqrt(pi)) [G - a^2 F'''/6 + a^4 F^(5)/120],
+//    dH/dx = E (-2x C - 2a S) - (2a/sqrt(pi)) [F'' - a^2 F^(4)/6 + a^4 F^(6)/120],
+//    dH/da = E (2a C - 2x S) - (2/sqrt(pi)) [G - a^2 F'''/2 + a^4 F^(5)/24],
+//    derivatives of Dawson's F as in voigt_core32; dH/du = sign(u) dH/dx.
+//  (the exp(-x^2) term of the wing form is kept for 6 <= |u| < 6.5)
+// ---------------------------------------------------------------------------
+struct VoigtGrad {
+    float h, hu, ha;
+};
+
+__device__ __forceinline__ VoigtGrad voigt_grad32(float u, const Voigt32 &c, const float2 *tab)
+{
+    VoigtGrad r;
+    const float x = fabsf(u);
+    const float sgn = u < 0.0f ? -1.0f : 1.0f;
+    if (x < 6.0f) {
+        float x0;
+        const int j = vtab_index(x, x0);
+        const float2 fg = tab[j];
+        const float d = x - x0;
+        const float m2x = -2.0f * x0;
+        const float f0 = fg.x, f1 = fg.y;
+        const float f2 = fmaf(m2x, f1, -2.0f * f0);
+        const float f3 = fmaf(m2x, f2, -4.0f * f1);
+        const float f4 = fmaf(m2x, f3, -6.0f * f2);
+        const float f5 = fmaf(m2x, f4, -8.0f * f3);
+        const float f6 = fmaf(m2x, f5, -10.0f * f4);
+        const float f7 = fmaf(m2x, f6, -12.0f * f5);
+        const float f8 = fmaf(m2x, f7, -14.0f * f6);
+        // F^(n)(x) = sum_m f_{n+m} d^m / m!
+        float g = f7 * (1.0f / 720.0f);
+        g = fmaf(g, d, f6 * (1.0f / 120.0f));
+        g = fmaf(g, d, f5 * (1.0f / 24.0f));
+        g = fmaf(g, d, f4 * (1.0f / 6.0f));
+        g = fmaf(g, d, f3 * 0.5f);
+        g = fmaf(g, d, f2);
+        g = fmaf(g, d, f1);
+        float F2 = f8 * (1.0f / 720.0f);
+        F2 = fmaf(F2, d, f7 * (1.0f / 120.0f));
+        F2 = fmaf(F2, d, f6 * (1.0f / 24.0f));
+        F2 = fmaf(F2, d, f5 * (1.0f / 6.0f));
+        F2 = fmaf(F2, d, f4 * 0.5f);
+        F2 = fmaf(F2, d, f3);
+        F2 = fmaf(F2, d, f2);
+        const float F3 = fmaf(fmaf(fmaf(fmaf(f7 * (1.0f / 24.0f), d, f6 * (1.0f / 6.0f)), d,
+                                        f5 * 0.5f), d, f4), d, f3);
+        const float F4 = fmaf(fmaf(fmaf(f7 * (1.0f / 6.0f), d, f6 * 0.5f), d, f5), d, f4);
+        const float F5 = fmaf(fmaf(f7 * 0.5f, d, f6), d, f5);
+        const float F6 = fmaf(f7, d, f6);
+        float S, C;
+        __sincosf(2.0f * x * c.a, &S, &C);
+        const float E = __expf(fmaf(-x, x, c.a2));
+        const float a4_120 = c.c5;                 // a^4 / 120
+        const float B = fmaf(a4_120, F5, fmaf(-c.c3, F3, g));
+        const float Bx = fmaf(a4_120, F6, fmaf(-c.c3, F4, F2));
+        const float Ba = fmaf(5.0f * a4_120, F5, fmaf(-3.0f * c.c3, F3, g));
+        r.h = fmaf(-c.two_a_sqpi, B, E * C);
+        const float dhdx = fmaf(-c.two_a_sqpi, Bx, E * fmaf(-2.0f * x, C, -2.0f * c.a * S));
+        r.hu = sgn * dhdx;
+        r.ha = fmaf(-1.12837916709551257f, Ba, E * fmaf(2.0f * c.a, C, -2.0f * x * S));
+        return r;
+    }
+    const float t = __fdividef(1.0f, u * u);
+    float p = 15836.1328125f, p1 = 253378.125f;
+    p = fmaf(p, t, 2111.484375f);
+    p1 = fmaf(p1, t, 29560.78125f);
+    p = fmaf(p, t, 324.84375f);
+    p1 = fmaf(p1, t, 3898.125f);
+    p = fmaf(p, t, 59.0625f);
+    p1 = fmaf(p1, t, 590.625f);
+    p = fmaf(p, t, 13.125f);
+    p1 = fmaf(p1, t, 105.0f);
+    p = fmaf(p, t, 3.75f);
+    p1 = fmaf(p1, t, 22.5f);
+    p = fmaf(p, t, 1.5f);
+    p1 = fmaf(p1, t, 6.0f);
+    p = fmaf(p, t, 1.0f);
+    p1 = fmaf(p1, t, 2.0f);
+    float q = 1082.8125f, q1 = 12993.75f;
+    q = fmaf(q, t, 157.5f);
+    q1 = fmaf(q1, t, 1575.0f);
+    q = fmaf(q, t, 26.25f);
+    q1 = fmaf(q1, t, 210.0f);
+    q = fmaf(q, t, 5.0f);
+    q1 = fmaf(q1, t, 30.0f);
+    q = fmaf(q, t, 1.0f);
+    q1 = fmaf(q1, t, 4.0f);
+    const float a2t = c.a2 * t;
+    r.h = c.a_sqpi * t * fmaf(-a2t, q, p);
+    r.hu = -c.a_sqpi * t * __fdividef(1.0f, u) * fmaf(-a2t, q1, p1);
+    r.ha = 0.56418958354775628f * t * fmaf(-3.0f * a2t, q, p);
+    if (x < 6.5f) {
+        float S, C;
+        __sincosf(2.0f * x * c.a, &S, &C);
+        const float E = __expf(fmaf(-x, x, c.a2));
+        r.h = fmaf(E, C, r.h);
+        r.hu = fmaf(sgn * E, fmaf(-2.0f * x, C, -2.0f * c.a * S), r.hu);
+        r.ha = fmaf(E, fmaf(2.0f * c.a, C, -2.0f * x * S), r.ha);
+    }
+    return r;
+}
+
+}  // namespace fsg

@@ -70,6 +70,70 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
     return out
 
 
+def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, vel, temp, h,
+                         axis, cofm, lines, precision="fp32", threads=0, persistent=-1):
+    """Several absorption lines in one call (one sightline search, one CUDA graph).
+
+    lines: sequence of (transition, dens, want_tau, want_colden) with
+    `transition` having lambda_cm/gamma/fosc/amumass and `dens` a float32 device
+    tensor.  Returns a list of (tau, colden) float64 device tensors (None where
+    not wanted)."""
+    import torch
+    axis, cofm = _host_tables(axis, cofm)
+    nlos = int(axis.shape[0])
+    arr = (_lib.Line * max(1, len(lines)))()
+    outs = []
+    for k, (t, dens, want_tau, want_colden) in enumerate(lines):
+        tau = torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device) \
+            if want_tau else None
+        col = torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device) \
+            if want_colden else None
+        arr[k].lambda_ = float(t.lambda_cm)
+        arr[k].gamma = float(t.gamma)
+        arr[k].fosc = float(t.fosc)
+        arr[k].amumass = float(t.amumass)
+        arr[k].dens = _dptr(dens, "float32", "dens")
+        arr[k].tau = _dptr(tau, "float64", "tau") if tau is not None else None
+        arr[k].colden = _dptr(col, "float64", "colden") if col is not None else None
+        outs.append((tau, col))
+    _bind_stream(ctx)
+    opt = _lib.make_options(precision, threads, persistent)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_spectra_batch_device(
+        ctx.handle, int(nbins), int(kernel), float(box), float(velfac), float(atime),
+        float(tautail), _dptr(pos, "float32", "pos"), _dptr(vel, "float32", "vel"),
+        _dptr(temp, "float32", "temp"), _dptr(h, "float32", "h"), int(pos.shape[0]),
+        axis.ctypes.data_as(ctypes.c_void_p), cofm.ctypes.data_as(ctypes.c_void_p), nlos,
+        len(lines), arr, ctypes.byref(opt), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return outs
+
+
+def tau_backward_device(ctx, nbins, kernel, box, velfac, atime, lam, gamma, fosc, amumass,
+                        tautail, pos, vel, dens, temp, h, axis, cofm, grad_tau):
+    """Gradients (d_dens, d_temp, d_vel) of L from dL/dtau, FP32, new float32 tensors."""
+    import torch
+    axis, cofm = _host_tables(axis, cofm)
+    gd = torch.zeros_like(dens)
+    gt = torch.zeros_like(temp)
+    gv = torch.zeros_like(vel)
+    grad_tau = grad_tau.contiguous()
+    _bind_stream(ctx)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_tau_backward_device(
+        ctx.handle, int(nbins), int(kernel), float(box), float(velfac), float(atime), float(lam),
+        float(gamma), float(fosc), float(amumass), float(tautail), _dptr(pos, "float32", "pos"),
+        _dptr(vel, "float32", "vel"), _dptr(dens, "float32", "dens"),
+        _dptr(temp, "float32", "temp"), _dptr(h, "float32", "h"), int(pos.shape[0]),
+        axis.ctypes.data_as(ctypes.c_void_p), cofm.ctypes.data_as(ctypes.c_void_p),
+        int(axis.shape[0]), _dptr(grad_tau, "float64", "grad_tau"), _dptr(gd, "float32", "gd"),
+        _dptr(gt, "float32", "gt"), _dptr(gv, "float32", "gv"), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return gd, gt, gv
+
+
 def build_pairs(ctx, box, pos, h, axis, cofm):
     """Sightline-particle search on the device; returns the number of pairs."""
     axis, cofm = _host_tables(axis, cofm)

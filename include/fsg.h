@@ -123,6 +123,47 @@ int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const
                            int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
                            int64_t *npairs, char *errbuf, size_t errlen);
 
+/*
+ * Batched form: several absorption lines of one snapshot in one call.  The
+ * reference needs one _Particle_Interpolate call per line and per quantity
+ * (spectra.py:801-831 compute_spectra, once per line; colden via
+ * compute_tau=0); here the sightline search runs once and every deposit of
+ * the call is captured in one CUDA graph.  Per line: its constants, its
+ * species density (DEVICE [npart], n_ion * rscale) and where to write tau
+ * and/or colden (DEVICE [nlos*nbins], NULL = not wanted).
+ */
+typedef struct {
+    double lambda, gamma, fosc, amumass;
+    const float *dens;
+    double *tau;
+    double *colden;
+} fsg_line;
+
+int fsg_spectra_batch_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
+                             double atime, double tautail, const float *pos, const float *vel,
+                             const float *temp, const float *h, int64_t npart,
+                             const int32_t *axis, const double *cofm, int32_t nlos, int nlines,
+                             const fsg_line *lines, const fsg_options *opt, char *errbuf,
+                             size_t errlen);
+
+/*
+ * Backward of the tau deposit (tuned FP32 form), for gradient-based fitting of
+ * particle fields; no counterpart call in the reference, whose tau is
+ * ParticleInterp::compute_tau (part_int.cpp:20-51).  Given dL/dtau
+ * (grad_tau, DEVICE [nlos*nbins] float64) it ADDS to grad_dens[npart],
+ * grad_temp[npart] and grad_vel[3*npart] (DEVICE float32; the component along
+ * each sightline's axis) the gradient of L with respect to dens, temp and the
+ * line-of-sight velocity.  The sightline search and the profiles are
+ * recomputed; the pixel windows and sub-sample counts are held fixed.
+ */
+int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
+                            double atime, double lambda, double gamma, double fosc,
+                            double amumass, double tautail, const float *pos, const float *vel,
+                            const float *dens, const float *temp, const float *h, int64_t npart,
+                            const int32_t *axis, const double *cofm, int32_t nlos,
+                            const double *grad_tau, float *grad_dens, float *grad_temp,
+                            float *grad_vel, char *errbuf, size_t errlen);
+
 /* Copy the context's pair lists to HOST buffers as CSR by sightline:
  * offsets[nlos+1], part[npairs], dr2[npairs].  Within a sightline the pairs
  * are sorted by ascending particle index (the std::map order of the
