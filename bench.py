@@ -39,10 +39,11 @@ sys.path.insert(0, ROOT)
 BASELINE_METRIC = ("Ly-α tau pixels/s, tuned FP32 vs plain FP64 GPU at max|ΔF|≤1e-4; "
                    "fwd+bwd ms")
 
-# Algorithmic flops per Voigt-profile evaluation, counted once from the source
-# of each branch (fsg_voigt.cuh) plus the 3-4 flops of the node sum in
-# tau_kern_inner; FMA = 2 flops, MUFU ops = 1.
-FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214}
+# Flops executed per Voigt-profile evaluation, counted once from the source of
+# each branch (fsg_voigt.cuh, fsg_deposit.cu) including the node sum of
+# tau_kern_inner; FMA = 2 flops, MUFU ops = 1.  Wing evaluations summed by the
+# multipole form cost 20 flops per pixel (7 evaluations): 20/7 each.
+FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
@@ -266,7 +267,9 @@ def main():
     # ---- work counts for the roofline (untimed counting variant)
     step("fp32", o=torch.empty_like(out), count=True)
     cnt = ctx.stats()
-    flops = sum(cnt["evals_" + k] * FLOPS_FP32[k] for k in ("core", "wing", "other"))
+    mp = cnt["evals_wing_multipole"]
+    flops = (cnt["evals_core"] * FLOPS_FP32["core"] + (cnt["evals_wing"] - mp) * FLOPS_FP32["wing"]
+             + cnt["evals_other"] * FLOPS_FP32["other"] + mp * FLOPS_FP32["multipole"])
     dep_mean = sum(dep_ms) / len(dep_ms)
     peak32 = _lib.fma_peak_tflops("fp32")
     achieved = flops / (dep_mean * 1e-3) / 1e12
@@ -289,8 +292,11 @@ def main():
                      "peak_source": "measured: libfsg FMA-chain microbenchmark (MEASURED_PEAKS.json "
                                     "has no FP32 figure)",
                      "work": {"evals_core": cnt["evals_core"], "evals_wing": cnt["evals_wing"],
+                              "evals_wing_multipole": mp,
                               "evals_other": cnt["evals_other"], "pixels": cnt["pixels"],
-                              "flops_per_eval": FLOPS_FP32},
+                              "flops_per_eval": FLOPS_FP32,
+                              "algorithmic_evals_per_s": (cnt["evals_core"] + cnt["evals_wing"]
+                                                          + cnt["evals_other"]) / (dep_mean * 1e-3)},
                      "traffic": None},
     }
 

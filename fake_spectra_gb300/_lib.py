@@ -55,7 +55,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("npairs", _c_i64), ("gpu_launches", _c_i64), ("fallback_lines", _c_i32),
                 ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d),
                 ("evals_core", _c_i64), ("evals_wing", _c_i64), ("evals_other", _c_i64),
-                ("pixels", _c_i64)]
+                ("pixels", _c_i64), ("evals_wing_multipole", _c_i64)]
 
 
 class Line(ctypes.Structure):
@@ -167,6 +167,7 @@ class Context:
         return self._h
 
     def set_stream(self, stream_ptr):
+        """Run on a cudaStream_t handle; 0/None is the CUDA default stream."""
         self._lib.fsg_context_set_stream(self._h, _p(stream_ptr) if stream_ptr else None)
 
     def stats(self):
@@ -176,7 +177,7 @@ class Context:
                 "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
                 "ms_deposit": float(s.ms_deposit), "evals_core": int(s.evals_core),
                 "evals_wing": int(s.evals_wing), "evals_other": int(s.evals_other),
-                "pixels": int(s.pixels)}
+                "pixels": int(s.pixels), "evals_wing_multipole": int(s.evals_wing_multipole)}
 
     def close(self):
         if self._h:

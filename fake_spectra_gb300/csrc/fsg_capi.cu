@@ -271,7 +271,8 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
     if (total > 0) {
         launch_emit_pairs(c->tables, p, perm, off, cur, part, dr2, err, s);
-        c->stats.gpu_launches++;
+        launch_check_emit(cnt, cur, nlos, err, s);
+        c->stats.gpu_launches += 2;
         cuda_check(cudaGetLastError(), "emit_pairs launch");
     }
     // sightline work order: descending pair count (largest first)
@@ -291,7 +292,8 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     c->stats.ms_search = ms;
     c->stats.npairs = total;
     if (h_err)
-        fail(FSG_ERR_DEVICE, "pair search reported device error bits 0x%x", h_err);
+        fail(FSG_ERR_DEVICE, "pair search reported device error bits 0x%x (%s)", h_err,
+             deverr_text(h_err).c_str());
 }
 
 // 3. deposit into out (device, nlos*nbins)
@@ -335,8 +337,8 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     const bool count = opt && opt->count_work;
     unsigned long long *ctr = nullptr;
     if (count) {
-        ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 4);
-        cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 4, s), "memset");
+        ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 5);
+        cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 5, s), "memset");
     }
     auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
     auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
@@ -367,15 +369,17 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
     c->stats.ms_deposit = ms;
     if (count) {
-        unsigned long long h_ctr[4];
+        unsigned long long h_ctr[5];
         cuda_check(cudaMemcpy(h_ctr, ctr, sizeof h_ctr, cudaMemcpyDeviceToHost), "read counters");
         c->stats.evals_core = (int64_t)h_ctr[0];
         c->stats.evals_wing = (int64_t)h_ctr[1];
         c->stats.evals_other = (int64_t)h_ctr[2];
         c->stats.pixels = (int64_t)h_ctr[3];
+        c->stats.evals_wing_multipole = (int64_t)h_ctr[4];
     }
     if (h_err)
-        fail(FSG_ERR_DEVICE, "deposit kernel reported device error bits 0x%x", h_err);
+        fail(FSG_ERR_DEVICE, "deposit kernel reported device error bits 0x%x (%s)", h_err,
+             deverr_text(h_err).c_str());
 }
 
 LineParams make_line_params(int compute_tau, int nbins, int kernel, double box, double velfac,
@@ -459,6 +463,10 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
     putp(c->axis.p);
     putp(c->pack.p);
     putp(gacc);
+    putp(ticket);
+    putp(bad);
+    putp(nbad);
+    putp(err);
     putp(p0.pos);
     putp(p0.vel);
     putp(p0.temp);
@@ -514,7 +522,8 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
     c->stats.ms_deposit = ms;
     if (h_err)
-        fail(FSG_ERR_DEVICE, "deposit kernels reported device error bits 0x%x", h_err);
+        fail(FSG_ERR_DEVICE, "deposit kernels reported device error bits 0x%x (%s)", h_err,
+             deverr_text(h_err).c_str());
 }
 
 fsg_context *g_default[64] = {nullptr};
@@ -609,7 +618,9 @@ int fsg_context_set_stream(fsg_context *ctx, void *cuda_stream)
 {
     if (!ctx)
         return FSG_ERR_VALUE;
-    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own;
+    // NULL is the CUDA default stream (handle 0), where torch runs unless told
+    // otherwise: work on it is ordered after the caller's pending kernels.
+    ctx->stream = (cudaStream_t)cuda_stream;
     return FSG_OK;
 }
 
@@ -797,7 +808,8 @@ int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box,
         cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
         ctx->stats.ms_deposit = ms;
         if (h_err)
-            fail(FSG_ERR_DEVICE, "backward kernel reported device error bits 0x%x", h_err);
+            fail(FSG_ERR_DEVICE, "backward kernel reported device error bits 0x%x (%s)", h_err,
+                 deverr_text(h_err).c_str());
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);

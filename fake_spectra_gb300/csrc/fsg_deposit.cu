@@ -220,12 +220,21 @@ struct PairInput {
     float dens, ppos, pvel, temp, smooth;
 };
 
+// A pair naming a particle outside [0, n) (pair lists that do not belong to
+// these particles) is flagged and read as an empty pair (h = 0), which every
+// deposit skips.
 __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLists &pl,
-                                               long long e, int axis, bool tau)
+                                               long long e, int axis, bool tau, unsigned *dev_err)
 {
     PairInput in;
     const int ip = pl.part[e];
     in.dr2 = pl.dr2[e];
+    if ((unsigned long long)(long long)ip >= (unsigned long long)p.n) {
+        atomicOr(dev_err, (unsigned)DEVERR_PAIR_INDEX);
+        in.dr2 = 1.0;
+        in.ppos = in.dens = in.smooth = in.pvel = in.temp = 0.f;
+        return in;
+    }
     const long long k = 3ll * ip + axis - 1;
     in.ppos = __ldg(&p.pos[k]);
     in.dens = __ldg(&p.dens[ip]);
@@ -240,9 +249,11 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
     return in;
 }
 
-// Work counters of the counting variant (per lane, reduced per CTA at exit).
+// Work counters of the counting variant (per lane, reduced per CTA at exit):
+// a core-branch evals, b wing-branch evals, c other evals, pixels, and d the
+// wing evals among b that were summed through the multipole form.
 struct Counters {
-    unsigned long long a, b, c, pixels;
+    unsigned long long a, b, c, pixels, d;
 };
 
 __device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ll); }
@@ -342,9 +353,31 @@ __device__ __noinline__ float voigt_wide32(float u, double a)
     return (float)voigt_f64((double)u, a);
 }
 
+// Far-wing multipole form of the 7-node sum.  In the wing every node profile
+// is the asymptotic series g(u) = sum_{j=1}^{8} gamma_j u^(-2j) (voigt_wing32,
+// gamma_j = a/sqrt(pi) (p_{j-1} - a^2 q_{j-2})).  The nodes are symmetric
+// (U_{8-i} = -U_i, equal weights), so with the even moments
+// M_m = sum_i w_i U_i^(2m) the binomial expansion of (U_i - V)^(-2j) gives
+//   sum_i w_i g(U_i - V) = sum_{r>=1} A_r V^(-2r),
+//   A_r = sum_{j=1}^{r} gamma_j C(2r-1, 2r-2j) M_{r-j}.
+// With R = 8 terms the truncation error is below 2e-7 relative once
+// |V| >= max(3.34 Umax, Umax + 6.5) (Umax = max |U_i|): one Horner polynomial
+// per pixel instead of seven profiles.
+constexpr int MP_R = 8;
+
+__host__ __device__ constexpr float binom_f(int n, int k)
+{
+    float r = 1.f;
+    for (int i = 1; i <= k; i++)
+        r = r * (float)(n - k + i) / (float)i;
+    return r;
+}
+
 struct Tau32 {
     Voigt32 vc;
     float U[NODES], w[NODES];   // node velocities / b and kernel weights
+    float A[MP_R];              // multipole coefficients (far wing)
+    float vmp;                  // |V| beyond which the multipole form holds
     float inv_b, base0, bintov, hbin_b, scale, scale_nod, sub_dv;
     float aa_f;
     double aa_d;
@@ -380,6 +413,39 @@ struct Tau32 {
             U[i - 1] = v * inv_b;
             w[i - 1] = node_weight<float>(lp.kernel, sqrtf(vdr2 + v * v) / vsmooth);
         }
+        {
+            float M[MP_R];
+#pragma unroll
+            for (int m = 0; m < MP_R; m++)
+                M[m] = 0.f;
+#pragma unroll
+            for (int i = 0; i < NODES; i++) {
+                const float u2 = U[i] * U[i];
+                float pw = w[i];
+#pragma unroll
+                for (int m = 0; m < MP_R; m++) {
+                    M[m] += pw;
+                    pw *= u2;
+                }
+            }
+            const float P[8] = {1.f, 1.5f, 3.75f, 13.125f, 59.0625f, 324.84375f,
+                                2111.484375f, 15836.1328125f};
+            const float Q[5] = {1.f, 5.f, 26.25f, 157.5f, 1082.8125f};
+            float gam[MP_R + 1];
+#pragma unroll
+            for (int j = 1; j <= MP_R; j++)
+                gam[j] = vc.a_sqpi * (P[j - 1] - (j >= 2 && j - 2 < 5 ? vc.a2 * Q[j - 2] : 0.f));
+#pragma unroll
+            for (int r = 1; r <= MP_R; r++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int j = 1; j <= r; j++)
+                    acc = fmaf(gam[j] * binom_f(2 * r - 1, 2 * r - 2 * j), M[r - j], acc);
+                A[r - 1] = acc;
+            }
+            const float umax = fabsf(U[0]);
+            vmp = fmaxf(3.34f * umax, umax + 6.5f);
+        }
         const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
         // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov)
         const double half_b = btherm / 2.;
@@ -409,6 +475,18 @@ struct Tau32 {
     {
         float total = 0.f;
         if (!wide) {
+            if (__all_sync(0xffffffffu, fabsf(V) >= vmp)) {
+                const float W = __fdividef(1.0f, V * V);
+                float sm = A[MP_R - 1];
+#pragma unroll
+                for (int r = MP_R - 2; r >= 0; r--)
+                    sm = fmaf(sm, W, A[r]);
+                if (COUNT) {
+                    ct.b += NODES;
+                    ct.d += NODES;
+                }
+                return sm * W;
+            }
             float u[NODES];
             bool wing = true, core = true;
 #pragma unroll
@@ -687,7 +765,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
             const int k = step + lane;
             const bool valid = k < half;
             const int koff = dir == 0 ? k : -1 - k;
-            Counters c1 = {0, 0, 0, 0};
+            Counters c1 = {0, 0, 0, 0, 0};
             R tl = (R)0;
             if constexpr (PREC == 0) {
                 if (valid)
@@ -705,6 +783,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
                     ct.a += c1.a;
                     ct.b += c1.b;
                     ct.c += c1.c;
+                    ct.d += c1.d;
                     ct.pixels++;
                 }
             }
@@ -743,7 +822,7 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
     Tau64 s;
     if (!s.setup(a.lp, in))
         return;
-    Counters c = {0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0};
     walk_tau<0, COUNT>(a, s, S, lo, hi, bad, lane, nullptr, c);
     if (COUNT) {
         ct.c += c.a + c.b + c.c;
@@ -763,7 +842,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     const int nbins = a.lp.nbins;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const double boxtokpc = a.lp.vbox / nbins / a.lp.velfac;
-    Counters ct = {0, 0, 0, 0};
+    Counters ct = {0, 0, 0, 0, 0};
     if constexpr (PREC == 1 && TAU)
         stage_voigt32(vtab);
 
@@ -781,7 +860,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         // 1. fixed-point scale from an upper bound of the sightline total
         double b = 0.0;
         for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-            const PairInput in = load_pair(a.p, a.pl, e, axis, TAU);
+            const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
             b += TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
         }
         const double B = block_sum(b, red);
@@ -804,7 +883,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         // 2. deposit: warp per pair
         if (!s_bad && B > 0.0) {
             for (long long e = e0 + warp; e < e1; e += nwarps) {
-                const PairInput in = load_pair(a.p, a.pl, e, axis, TAU);
+                const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
                 if constexpr (TAU) {
                     if constexpr (PREC == 0) {
                         Tau64 s;
@@ -856,6 +935,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         atomicAdd(&a.counters[1], ct.b);
         atomicAdd(&a.counters[2], ct.c);
         atomicAdd(&a.counters[3], ct.pixels);
+        atomicAdd(&a.counters[4], ct.d);
     }
 }
 
@@ -877,9 +957,9 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
     const double boxtokpc = lp.vbox / nbins / lp.velfac;
     double *row = out + (size_t)line * nbins;
     const long long e0 = pl.off[line], e1 = pl.off[line + 1];
-    Counters ct = {0, 0, 0, 0};
+    Counters ct = {0, 0, 0, 0, 0};
     for (long long e = e0 + warp; e < e1; e += nwarps) {
-        const PairInput in = load_pair(p, pl, e, axis, TAU);
+        const PairInput in = load_pair(p, pl, e, axis, TAU, dev_err);
         if (TAU) {
             Tau64 s;
             if (!s.setup(lp, in))
@@ -981,7 +1061,7 @@ __device__ __noinline__ void grad_pair_careful(const GradArgs &a, const PairInpu
     const double amp_v = s.ampd / a.lp.velfac;   // amp dens / velfac
     const double amp_nod = (s.ampd / ((double)in.dens != 0.0 ? (double)in.dens : 1.0)) /
                            a.lp.velfac;
-    Counters ct = {0, 0, 0, 0};
+    Counters ct = {0, 0, 0, 0, 0};
     for (int dir = 0; dir < 2; dir++) {
         for (int step = 0; step < half; step += 32) {
             const int k = step + lane;
@@ -1046,7 +1126,7 @@ __global__ void __launch_bounds__(512) grad_kernel(GradArgs a)
         const double *gt = a.grad_tau + (size_t)line * nbins;
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
         for (long long e = e0 + warp; e < e1; e += nwarps) {
-            const PairInput in = load_pair(a.p, a.pl, e, axis, true);
+            const PairInput in = load_pair(a.p, a.pl, e, axis, true, a.dev_err);
             const int ip = a.pl.part[e];
             Tau32 s;
             if (!s.setup(a.lp, in))

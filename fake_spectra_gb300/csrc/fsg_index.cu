@@ -384,6 +384,14 @@ __global__ void cell_scatter_kernel(const unsigned *key, unsigned *cursor, int *
     }
 }
 
+__global__ void check_emit_kernel(const unsigned long long *line_count,
+                                  const unsigned long long *cursor, int nlos, unsigned *dev_err)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l < nlos && cursor[l] != line_count[l])
+        atomicOr(dev_err, (unsigned)DEVERR_PAIR_COUNT);
+}
+
 int search_grid(long long n)
 {
     int dev = 0, sms = 0;
@@ -414,6 +422,14 @@ void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
         return;
     emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, off, cursor, part, dr2,
                                                        dev_err);
+}
+
+void launch_check_emit(const unsigned long long *line_count, const unsigned long long *cursor,
+                       int nlos, unsigned *dev_err, cudaStream_t s)
+{
+    if (nlos <= 0)
+        return;
+    check_emit_kernel<<<(nlos + 255) / 256, 256, 0, s>>>(line_count, cursor, nlos, dev_err);
 }
 
 // ~64 particles per cell, at most 128^3 cells (the totals then fit one scan block)

@@ -11,6 +11,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <string>
 
 namespace fsg {
 
@@ -38,7 +39,22 @@ enum DeviceError : unsigned {
     DEVERR_FIXED_OVERFLOW = 1u,   // a contribution exceeded its sightline's fixed-point range
     DEVERR_PAIR_SLOT = 2u,        // emit pass found more pairs than the count pass
     DEVERR_WINDOW_LIMIT = 4u,     // a pixel window or sub-sample count beyond the limits below
+    DEVERR_PAIR_COUNT = 8u,       // emit pass wrote fewer pairs of a sightline than counted
+    DEVERR_PAIR_INDEX = 16u,      // a pair names a particle outside [0, n) (pair skipped)
 };
+
+// Names of the set bits, for error messages ("fixed-point overflow, ...").
+inline std::string deverr_text(unsigned bits)
+{
+    static const char *names[] = {"fixed-point overflow", "pair slot overflow",
+                                  "window or sub-sample limit", "pair count mismatch",
+                                  "pair particle index out of range"};
+    std::string r;
+    for (int b = 0; b < 5; b++)
+        if (bits & (1u << b))
+            r += (r.empty() ? "" : ", ") + std::string(names[b]);
+    return r.empty() ? "unknown" : r;
+}
 
 // Limits that turn inputs on which the reference loops for ever (or has
 // undefined behaviour: T = 0, h = inf) into an error instead of a hang.
@@ -117,6 +133,10 @@ void launch_count_pairs(const LineTables &t, const Particles &p, const int *perm
 void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
                        const long long *off, unsigned long long *cursor, int *part, double *dr2,
                        unsigned *dev_err, cudaStream_t s);
+// After emit: every sightline's cursor must equal its count (DEVERR_PAIR_COUNT
+// otherwise), so no slot of the pair lists is left unwritten.
+void launch_check_emit(const unsigned long long *line_count, const unsigned long long *cursor,
+                       int nlos, unsigned *dev_err, cudaStream_t s);
 
 // Counting sort of the particles by a G^3 spatial cell, so that the search
 // visits neighbouring particles together.  Scratch: key[N], perm[N] (output),
@@ -136,8 +156,8 @@ struct DepositLaunch {
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
 // whose contributions are not all finite are appended to bad_lines (counter
 // *n_bad) and left for deposit_fallback.
-// counters (may be null): launches the counting variant, which adds
-// {core-branch evals, wing-branch evals, other evals, pixels} into counters[0..3].
+// counters (may be null): launches the counting variant, which adds {core-branch
+// evals, wing-branch evals, other evals, pixels, multipole wing evals} into counters[0..4].
 void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
                     const PairLists &pl, const int *line_order, int nlos, double *out,
                     unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,

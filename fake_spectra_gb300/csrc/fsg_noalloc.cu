@@ -281,6 +281,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     NA_CUDA(cudaMemsetAsync(d_err, 0, 4, s), "memset");
     if (total > 0) {
         launch_emit_pairs(t, p, nullptr, d_off, d_cursor, d_part, d_dr2, d_err, s);
+        launch_check_emit(d_count, d_cursor, nlos, d_err, s);
         NA_CUDA(cudaGetLastError(), "emit_pairs launch");
     }
     for (int i = 0; i < nlos; i++)
@@ -324,7 +325,8 @@ extern "C" int fsg_particle_interpolate_noalloc(
     NA_CUDA(cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, s), "read");
     NA_CUDA(cudaStreamSynchronize(s), "deposit");
     if (h_err)
-        return set_error(errbuf, errlen, FSG_ERR_DEVICE, "kernels reported device error bits 0x%x",
-                         h_err);
+        return set_error(errbuf, errlen, FSG_ERR_DEVICE,
+                         "kernels reported device error bits 0x%x (%s)", h_err,
+                         deverr_text(h_err).c_str());
     return FSG_OK;
 }

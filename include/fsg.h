@@ -63,6 +63,8 @@ typedef struct {
     int64_t evals_wing;      /* asymptotic branch                               */
     int64_t evals_other;     /* a == 0, a < 0 or a > 0.1 (FP32: FP64 profile)   */
     int64_t pixels;          /* pixel contributions                             */
+    int64_t evals_wing_multipole; /* wing evaluations summed by the far-wing
+                                     multipole form (FP32; subset of evals_wing) */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
@@ -79,7 +81,11 @@ int fsg_measure_fma_peak(int precision, double *tflops, char *errbuf, size_t err
  * lists of the last search. */
 int fsg_context_create(int device, fsg_context **ctx, char *errbuf, size_t errlen);
 void fsg_context_destroy(fsg_context *ctx);
-/* Use a caller-owned cudaStream_t (NULL = the context's own stream). */
+/* Run the context's work on a caller's cudaStream_t; NULL is the CUDA default
+ * stream (handle 0, torch's default).  Until the first call a context runs on
+ * a non-blocking stream of its own, which is not ordered with the default
+ * stream: a caller whose inputs are produced on another stream binds that
+ * stream here first. */
 int fsg_context_set_stream(fsg_context *ctx, void *cuda_stream);
 int fsg_context_stats(const fsg_context *ctx, fsg_stats *out);
 
