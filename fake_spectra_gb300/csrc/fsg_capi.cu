@@ -296,6 +296,8 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
              deverr_text(h_err).c_str());
 }
 
+DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt);
+
 // 3. deposit into out (device, nlos*nbins)
 void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
              const fsg_options *opt)
@@ -314,22 +316,7 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
         return;
     }
     PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
-    DepositLaunch cfg{};
-    cfg.precision = opt ? opt->precision : FSG_PREC_FP64;
-    if (cfg.precision != FSG_PREC_FP64 && cfg.precision != FSG_PREC_FP32)
-        fail(FSG_ERR_VALUE, "unknown precision %d", cfg.precision);
-    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
-    cfg.threads = (opt && opt->threads > 0) ? opt->threads : tmax;
-    if (cfg.threads % 32 || cfg.threads > tmax)
-        fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
-    cfg.smem_mode = lp.nbins <= deposit_max_smem_bins();
-    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent
-                                                    : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int per_sm = std::max(1, deposit_resident_ctas(lp.compute_tau, cfg.precision,
-                                                         cfg.threads, lp.nbins, cfg.smem_mode));
-    cfg.grid = std::min(nlos, sms * per_sm);
+    const DepositLaunch cfg = deposit_config(c, lp, opt);
     unsigned long long *gacc = nullptr;
     if (!cfg.smem_mode) {
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
@@ -415,13 +402,12 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
     cfg.threads = (opt && opt->threads > 0) ? opt->threads : tmax;
     if (cfg.threads % 32 || cfg.threads > tmax)
         fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
-    cfg.smem_mode = lp.nbins <= deposit_max_smem_bins();
+    deposit_plan(cfg, lp.compute_tau, lp.nbins);
     cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent
                                                     : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    const int per_sm = std::max(1, deposit_resident_ctas(lp.compute_tau, cfg.precision,
-                                                         cfg.threads, lp.nbins, cfg.smem_mode));
+    const int per_sm = std::max(1, deposit_resident_ctas(cfg, lp.compute_tau, lp.nbins));
     cfg.grid = std::min(c->nlos, sms * per_sm);
     return cfg;
 }

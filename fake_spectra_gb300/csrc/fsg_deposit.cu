@@ -336,6 +336,8 @@ struct Tau64 {
         return total / (npoints - 1);
     }
 
+    __device__ __forceinline__ int bin0(int nbins_) const { return wrap_bin(zmax, nbins_); }
+
     // pixel z = zmax + koff
     template <bool COUNT>
     __device__ __forceinline__ double taulast(int koff, unsigned *dev_err, Counters &ct) const
@@ -346,13 +348,6 @@ struct Tau64 {
 };
 
 // ------------------------------------------------ FP32 (tuned form) pair
-// Profiles with a outside [0, 0.1] (very cold gas, negative damping) use the
-// FP64 profile; kept out of line so the FP32 hot loop stays small.
-__device__ __noinline__ float voigt_wide32(float u, double a)
-{
-    return (float)voigt_f64((double)u, a);
-}
-
 // Far-wing multipole form of the 7-node sum.  In the wing every node profile
 // is the asymptotic series g(u) = sum_{j=1}^{8} gamma_j u^(-2j) (voigt_wing32,
 // gamma_j = a/sqrt(pi) (p_{j-1} - a^2 q_{j-2})).  The nodes are symmetric
@@ -373,6 +368,115 @@ __host__ __device__ constexpr float binom_f(int n, int k)
     return r;
 }
 
+// Per-pair constants of the FP32 form.  One lane computes one pair (the FP64
+// parts: the pixel of the particle velocity and its offset, the thermal width,
+// the sub-sample count), so a warp sets up 32 pairs for the FP64 cost of one;
+// the warp then walks the staged pairs one after another.
+constexpr int STAGE_CAREFUL = 1 << 30;   // walk in FP64 (see below)
+constexpr int STAGE_SKIP = 1 << 29;      // no overlap (hh^2 <= dr2) or no pair
+constexpr int STAGE_NP = (1 << 29) - 1;  // sub-sample count bits
+
+struct __align__(16) Stage32 {
+    int j0;                  // bin of pixel zmax = floor(v_particle / pixel width)
+    int flags;               // npoints | STAGE_CAREFUL | STAGE_SKIP
+    float base0;             // velocity of pixel zmax's low edge - v_particle
+    float inv_b;             // 1 / b
+    float scale;             // amp dens / velfac x node spacing / (npoints - 1)
+    float aa;                // damping parameter a = voigt_fac / b
+    float u1;                // node spacing / b: node i sits at U_i = (i - 4) u1
+    float vmp;               // |V| beyond which the multipole form holds
+    float w[4];              // kernel weights of nodes 1..4 (nodes 5..7 mirror 3..1)
+    float A[MP_R];           // far-wing multipole coefficients
+};
+static_assert(sizeof(Stage32) == 80, "Stage32 is five 16-byte words");
+
+// SingleAbsorber (singleabs.h:81-90) and the per-particle constants of
+// add_tau_particle (absorption.cpp:225-247), FP32 form.  Returns false for a
+// pair whose smoothing sphere misses the sightline (absorption.cpp:232).
+// scale_nod (may be null) receives scale without the density factor.
+__device__ __forceinline__ bool stage32_setup(const LineParams &lp, const PairInput &in,
+                                              double bintov_d, Stage32 &st, float *scale_nod)
+{
+    const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+    if (hh2 - in.dr2 <= 0)
+        return false;
+    const double btherm = lp.bfac * sqrt((double)in.temp);
+    const double vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
+    const long long zmax = (long long)floor(vel / bintov_d);
+    st.j0 = wrap_bin(zmax, lp.nbins);
+    st.base0 = (float)((double)zmax * bintov_d - vel);   // FP64 offset of pixel zmax
+    const float b = (float)btherm;
+    st.inv_b = 1.0f / b;
+    const double aa_d = lp.voigt_fac / btherm;
+    st.aa = (float)aa_d;
+    const bool wide = !(aa_d >= 0.0 && aa_d <= 0.1);
+    const float vdr2 = (float)((lp.velfac * in.dr2) * lp.velfac);
+    const float vsmooth = (float)(lp.velfac * (double)in.smooth);
+    const float vhigh = (vsmooth * vsmooth > vdr2 ? sqrtf(vsmooth * vsmooth - vdr2) : 0.f);
+    const float deltav = 2.f * vhigh / NGRID;
+#pragma unroll
+    for (int i = 1; i <= 4; ++i) {
+        const float v = (float)i * deltav - vhigh;
+        st.w[i - 1] = node_weight<float>(lp.kernel, sqrtf(vdr2 + v * v) / vsmooth);
+    }
+    st.u1 = deltav * st.inv_b;
+    {
+        // even moments M_m = sum_i w_i U_i^(2m): nodes i and 8-i share |U_i| and w_i,
+        // the centre node (U = 0) only enters M_0
+        const float q1 = st.u1 * st.u1, q2 = 4.f * q1, q3 = 9.f * q1;
+        float M[MP_R];
+        M[0] = 2.f * (st.w[0] + st.w[1] + st.w[2]) + st.w[3];
+        float p1 = st.w[2], p2 = st.w[1], p3 = st.w[0];
+#pragma unroll
+        for (int m = 1; m < MP_R; m++) {
+            p1 *= q1;
+            p2 *= q2;
+            p3 *= q3;
+            M[m] = 2.f * (p1 + p2 + p3);
+        }
+        const Voigt32 vc = make_voigt32(st.aa);
+        const float P[8] = {1.f, 1.5f, 3.75f, 13.125f, 59.0625f, 324.84375f,
+                            2111.484375f, 15836.1328125f};
+        const float Q[5] = {1.f, 5.f, 26.25f, 157.5f, 1082.8125f};
+        float gam[MP_R + 1];
+#pragma unroll
+        for (int j = 1; j <= MP_R; j++)
+            gam[j] = vc.a_sqpi * (P[j - 1] - (j >= 2 && j - 2 < 5 ? vc.a2 * Q[j - 2] : 0.f));
+#pragma unroll
+        for (int r = 1; r <= MP_R; r++) {
+            float acc = 0.f;
+#pragma unroll
+            for (int j = 1; j <= r; j++)
+                acc = fmaf(gam[j] * binom_f(2 * r - 1, 2 * r - 2 * j), M[r - j], acc);
+            st.A[r - 1] = acc;
+        }
+        const float umax = 3.f * fabsf(st.u1);
+        st.vmp = fmaxf(3.34f * umax, umax + 6.5f);
+    }
+    const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
+    // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov)
+    const double half_b = btherm / 2.;
+    double npd = 1.0;
+    if (!(bintov_d < half_b))
+        npd = 2 * ceil(bintov_d / half_b / 2) + 1.;
+    if (!(npd <= MAX_SUBSAMPLES))
+        npd = MAX_SUBSAMPLES + 1;   // flagged by the FP64 walk
+    const int npoints = (int)npd;
+    // Float node offsets keep ~1e-5 absolute accuracy only while |U_i| <= 256;
+    // sub-sampled, very narrow or wide (a outside [0, 0.1]) profiles take the
+    // FP64 walk.
+    const bool careful = wide || npoints > 8 || (double)vhigh > 256.0 * btherm;
+    double sc = amp / lp.velfac * (double)deltav;
+    if (npoints > 1)
+        sc /= (npoints - 1);
+    if (scale_nod)
+        *scale_nod = (float)sc;
+    st.scale = (float)(sc * (double)in.dens);
+    st.flags = npoints | (careful ? STAGE_CAREFUL : 0);
+    return true;
+}
+
+// The FP32 walk of one pair, built from its staged constants (all lanes).
 struct Tau32 {
     Voigt32 vc;
     float U[NODES], w[NODES];   // node velocities / b and kernel weights
@@ -380,151 +484,101 @@ struct Tau32 {
     float vmp;                  // |V| beyond which the multipole form holds
     float inv_b, base0, bintov, hbin_b, scale, scale_nod, sub_dv;
     float aa_f;
-    double aa_d;
-    long long zmax;
+    int j0;
     int npoints;                 // 1: midpoint; else trapezoid points (uniform per pair)
-    bool wide;                   // a > 0.1 or a < 0: profile evaluated in FP64
-    bool careful;                // b far below the pixel or smoothing width: FP64 pair walk
+    bool careful;                // walk in FP64 instead (Stage32 flags)
 
+    __device__ __forceinline__ void load(const Stage32 &st, float bintov_f)
+    {
+        j0 = st.j0;
+        base0 = st.base0;
+        inv_b = st.inv_b;
+        scale = st.scale;
+        scale_nod = 0.f;
+        aa_f = st.aa;
+        vc = make_voigt32(aa_f);
+#pragma unroll
+        for (int i = 0; i < NODES; ++i)
+            U[i] = (float)(i - 3) * st.u1;
+        w[0] = w[6] = st.w[0];
+        w[1] = w[5] = st.w[1];
+        w[2] = w[4] = st.w[2];
+        w[3] = st.w[3];
+#pragma unroll
+        for (int r = 0; r < MP_R; ++r)
+            A[r] = st.A[r];
+        vmp = st.vmp;
+        bintov = bintov_f;
+        hbin_b = 0.5f * bintov * inv_b;
+        npoints = st.flags & STAGE_NP;
+        careful = (st.flags & STAGE_CAREFUL) != 0;
+        sub_dv = npoints > 1 ? __fdividef(bintov, (float)(npoints - 1)) * inv_b : 0.f;
+    }
+
+    // Setup of one pair by every lane (the backward kernel).
     __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
     {
-        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-        if (hh2 - in.dr2 <= 0)
-            return false;
-        const double btherm = lp.bfac * sqrt((double)in.temp);
-        const double vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
         const double bintov_d = lp.vbox / lp.nbins;
-        zmax = (long long)floor(vel / bintov_d);
-        base0 = (float)((double)zmax * bintov_d - vel);   // FP64 offset of pixel zmax
-        bintov = (float)bintov_d;
-        const float b = (float)btherm;
-        inv_b = 1.0f / b;
-        aa_d = lp.voigt_fac / btherm;
-        aa_f = (float)aa_d;
-        wide = !(aa_d >= 0.0 && aa_d <= 0.1);
-        vc = make_voigt32(aa_f);
-        const float vdr2 = (float)((lp.velfac * in.dr2) * lp.velfac);
-        const float vsmooth = (float)(lp.velfac * (double)in.smooth);
-        const float vhigh = (vsmooth * vsmooth > vdr2 ? sqrtf(vsmooth * vsmooth - vdr2) : 0.f);
-        const float deltav = 2.f * vhigh / NGRID;
-#pragma unroll
-        for (int i = 1; i < NGRID; ++i) {
-            const float v = (float)i * deltav - vhigh;
-            U[i - 1] = v * inv_b;
-            w[i - 1] = node_weight<float>(lp.kernel, sqrtf(vdr2 + v * v) / vsmooth);
-        }
-        {
-            float M[MP_R];
-#pragma unroll
-            for (int m = 0; m < MP_R; m++)
-                M[m] = 0.f;
-#pragma unroll
-            for (int i = 0; i < NODES; i++) {
-                const float u2 = U[i] * U[i];
-                float pw = w[i];
-#pragma unroll
-                for (int m = 0; m < MP_R; m++) {
-                    M[m] += pw;
-                    pw *= u2;
-                }
-            }
-            const float P[8] = {1.f, 1.5f, 3.75f, 13.125f, 59.0625f, 324.84375f,
-                                2111.484375f, 15836.1328125f};
-            const float Q[5] = {1.f, 5.f, 26.25f, 157.5f, 1082.8125f};
-            float gam[MP_R + 1];
-#pragma unroll
-            for (int j = 1; j <= MP_R; j++)
-                gam[j] = vc.a_sqpi * (P[j - 1] - (j >= 2 && j - 2 < 5 ? vc.a2 * Q[j - 2] : 0.f));
-#pragma unroll
-            for (int r = 1; r <= MP_R; r++) {
-                float acc = 0.f;
-#pragma unroll
-                for (int j = 1; j <= r; j++)
-                    acc = fmaf(gam[j] * binom_f(2 * r - 1, 2 * r - 2 * j), M[r - j], acc);
-                A[r - 1] = acc;
-            }
-            const float umax = fabsf(U[0]);
-            vmp = fmaxf(3.34f * umax, umax + 6.5f);
-        }
-        const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
-        // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov)
-        const double half_b = btherm / 2.;
-        double npd = 1.0;
-        if (!(bintov_d < half_b))
-            npd = 2 * ceil(bintov_d / half_b / 2) + 1.;
-        if (!(npd <= MAX_SUBSAMPLES))
-            npd = MAX_SUBSAMPLES + 1;   // flagged in taulast
-        npoints = (int)npd;
-        // Float node offsets U_i = v_i / b keep ~1e-5 absolute accuracy only while
-        // |U_i| <= 256; sub-sampled or very narrow profiles take the FP64 walk.
-        careful = wide || npoints > 8 || (double)vhigh > 256.0 * btherm;
-        double sc = amp / lp.velfac * (double)deltav;
-        if (npoints > 1)
-            sc /= (npoints - 1);
-        scale_nod = (float)sc;
-        scale = (float)(sc * (double)in.dens);
-        hbin_b = 0.5f * bintov * inv_b;
-        sub_dv = npoints > 1 ? (float)(bintov_d / (npoints - 1)) * inv_b : 0.f;
+        Stage32 st;
+        float snod;
+        if (!stage32_setup(lp, in, bintov_d, st, &snod))
+            return false;
+        load(st, (float)bintov_d);
+        scale_nod = snod;
         return true;
     }
+
+    __device__ __forceinline__ int bin0(int) const { return j0; }
 
     // Called by every lane of the warp (lanes past the window compute and
     // discard), so the warp votes below see a converged warp.
     template <bool COUNT>
     __device__ __forceinline__ float inner(float V, const float2 *tab, Counters &ct) const
     {
-        float total = 0.f;
-        if (!wide) {
-            if (__all_sync(0xffffffffu, fabsf(V) >= vmp)) {
-                const float W = __fdividef(1.0f, V * V);
-                float sm = A[MP_R - 1];
+        if (__all_sync(0xffffffffu, fabsf(V) >= vmp)) {
+            const float W = __fdividef(1.0f, V * V);
+            float sm = A[MP_R - 1];
 #pragma unroll
-                for (int r = MP_R - 2; r >= 0; r--)
-                    sm = fmaf(sm, W, A[r]);
-                if (COUNT) {
-                    ct.b += NODES;
-                    ct.d += NODES;
-                }
-                return sm * W;
-            }
-            float u[NODES];
-            bool wing = true, core = true;
-#pragma unroll
-            for (int i = 0; i < NODES; ++i) {
-                u[i] = U[i] - V;
-                wing &= fabsf(u[i]) >= 6.5f;
-                core &= fabsf(u[i]) < 6.0f;
-            }
-            if (__all_sync(0xffffffffu, wing)) {
-#pragma unroll
-                for (int i = 0; i < NODES; ++i)
-                    total = fmaf(voigt_wing32(u[i], vc), w[i], total);
-                if (COUNT)
-                    ct.b += NODES;
-                return total;
-            }
-            if (__all_sync(0xffffffffu, core)) {
-#pragma unroll
-                for (int i = 0; i < NODES; ++i)
-                    total = fmaf(voigt_core32(u[i], vc, tab), w[i], total);
-                if (COUNT)
-                    ct.a += NODES;
-                return total;
-            }
-            unsigned nn = 0;
-#pragma unroll
-            for (int i = 0; i < NODES; ++i)
-                total = fmaf(voigt_f32<COUNT>(u[i], vc, tab, nn), w[i], total);
+            for (int r = MP_R - 2; r >= 0; r--)
+                sm = fmaf(sm, W, A[r]);
             if (COUNT) {
-                ct.a += nn;
-                ct.b += NODES - nn;
+                ct.b += NODES;
+                ct.d += NODES;
             }
-        } else {
+            return sm * W;
+        }
+        float total = 0.f;
+        float u[NODES];
+        bool wing = true, core = true;
+#pragma unroll
+        for (int i = 0; i < NODES; ++i) {
+            u[i] = U[i] - V;
+            wing &= fabsf(u[i]) >= 6.5f;
+            core &= fabsf(u[i]) < 6.0f;
+        }
+        if (__all_sync(0xffffffffu, wing)) {
 #pragma unroll
             for (int i = 0; i < NODES; ++i)
-                total = fmaf((float)voigt_wide32(U[i] - V, aa_d), w[i], total);
+                total = fmaf(voigt_wing32(u[i], vc), w[i], total);
             if (COUNT)
-                ct.c += NODES;
+                ct.b += NODES;
+            return total;
+        }
+        if (__all_sync(0xffffffffu, core)) {
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                total = fmaf(voigt_core32(u[i], vc, tab), w[i], total);
+            if (COUNT)
+                ct.a += NODES;
+            return total;
+        }
+        unsigned nn = 0;
+#pragma unroll
+        for (int i = 0; i < NODES; ++i)
+            total = fmaf(voigt_f32<COUNT>(u[i], vc, tab, nn), w[i], total);
+        if (COUNT) {
+            ct.a += nn;
+            ct.b += NODES - nn;
         }
         return total;
     }
@@ -539,10 +593,6 @@ struct Tau32 {
         const float vlow_b = fmaf(k, bintov, base0) * inv_b;   // (v_low - v_particle) / b
         if (npoints == 1)
             return scale * inner<COUNT>(vlow_b + hbin_b, tab, ct);
-        if (npoints > (int)MAX_SUBSAMPLES) {
-            atomicOr(dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
-            return __int_as_float(0x7fc00000);
-        }
         float total = 0.5f * inner<COUNT>(vlow_b, tab, ct);
         for (int i = 1; i < npoints - 1; ++i)
             total += inner<COUNT>(fmaf((float)i, sub_dv, vlow_b), tab, ct);
@@ -550,6 +600,34 @@ struct Tau32 {
         return scale * total;
     }
 };
+
+// Float constants of tau_pair_bound32 (computed once per thread).
+struct Bound32 {
+    float bfac, voigt_fac, velfac_abs, ampc, kfac;
+    __device__ __forceinline__ explicit Bound32(const LineParams &lp)
+    {
+        bfac = (float)lp.bfac;
+        voigt_fac = (float)lp.voigt_fac;
+        velfac_abs = (float)fabs(lp.velfac);
+        ampc = (float)(lp.sigma_a / sqrt(PI_D) * LIGHT_KMS / fabs(lp.velfac));
+        kfac = (float)(2.0 / NGRID * 7.0 * kernel_max(lp.kernel) * 1.001);
+    }
+};
+
+// tau_pair_bound in FP32 arithmetic with a 1e-3 margin (the FP32 form's
+// contributions are FP32 values too): no FP64 work per pair beyond the overlap
+// test, which follows the reference's double comparison.
+__device__ __forceinline__ double tau_pair_bound32(const Bound32 &k, const PairInput &in)
+{
+    const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+    if (hh2 - in.dr2 <= 0)
+        return 0.0;
+    const float btherm = k.bfac * sqrtf(in.temp);
+    const float aa = k.voigt_fac / btherm;
+    const float hmax = aa >= 0.f ? 1.f : 2.f * expf(aa * aa) + 1.f;
+    return (double)(fabsf(k.ampc / btherm * in.dens) * (k.velfac_abs * fabsf(in.smooth)) *
+                    k.kfac * hmax);
+}
 
 // Upper bound of |taulast| for a pair (any pixel): |amp dens/velfac| x deltav x
 // 7 x max|kernel weight| x max H, with H <= 1 for a >= 0.
@@ -711,9 +789,10 @@ struct DepositArgs {
     int *n_bad;
     unsigned *dev_err;
     unsigned long long *gacc;   // global accumulators when not in shared memory
-    unsigned long long *counters;   // [4] (counting variant only)
+    unsigned long long *counters;   // [5] (counting variant only)
     int smem_mode;
     int persistent;
+    int chunk;                      // pairs staged per warp (FP32 tau form)
 };
 
 template <class R>
@@ -755,7 +834,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
     const int nbins = a.lp.nbins;
     const int half = nbins / 2;
     const R tautail = (R)a.lp.tautail;
-    const int j0 = wrap_bin(s.zmax, nbins);
+    const int j0 = s.bin0(nbins);
     const float lane_f = (float)lane;
     for (int dir = 0; dir < 2; dir++) {
         // kf tracks (float)koff exactly (integers below 2^24) without conversions
@@ -830,21 +909,73 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
     }
 }
 
+// FP32 tau form: the warps of the CTA take chunks of `chunk` consecutive pairs
+// of the sightline from a shared counter (dynamic balance: pair costs differ by
+// orders of magnitude); each lane sets up one pair of the chunk into the warp's
+// staging area, then the warp walks the chunk's pairs one after another.
+template <bool COUNT>
+__device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, long long e0,
+                                                long long e1, int S, unsigned long long *lo,
+                                                unsigned long long *hi, int *bad,
+                                                Stage32 *sw, unsigned *s_chunk,
+                                                const float2 *vtab, double bintov_d, int lane,
+                                                Counters &ct)
+{
+    const int chunk = a.chunk;
+    const float bintov_f = (float)bintov_d;
+    for (;;) {
+        unsigned c = 0;
+        if (lane == 0)
+            c = atomicAdd(s_chunk, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        const long long cb = e0 + (long long)c * chunk;
+        if (cb >= e1)
+            break;
+        const int n = (int)min((long long)chunk, e1 - cb);
+        if (lane < n) {
+            const PairInput in = load_pair(a.p, a.pl, cb + lane, axis, true, a.dev_err);
+            Stage32 st;
+            if (!stage32_setup(a.lp, in, bintov_d, st, nullptr))
+                st.flags = STAGE_SKIP;
+            sw[lane] = st;
+        }
+        __syncwarp();
+        for (int k = 0; k < n; k++) {
+            const Stage32 st = sw[k];
+            if (st.flags & STAGE_SKIP)
+                continue;
+            if (st.flags & STAGE_CAREFUL) {
+                const PairInput in = load_pair(a.p, a.pl, cb + k, axis, true, a.dev_err);
+                walk_tau_careful<COUNT>(a, in, S, lo, hi, bad, lane, ct);
+                continue;
+            }
+            Tau32 s;
+            s.load(st, bintov_f);
+            walk_tau<1, COUNT>(a, s, S, lo, hi, bad, lane, vtab, ct);
+        }
+        __syncwarp();
+    }
+}
+
 template <bool TAU, int PREC, bool COUNT>
 __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     deposit_kernel(DepositArgs a)
 {
-    extern __shared__ unsigned long long smem[];
+    extern __shared__ __align__(16) unsigned long long smem[];
     __shared__ double red[32];
     __shared__ float2 vtab[FSG_V32_N];
     __shared__ int s_bad;
-    __shared__ unsigned s_ticket;
+    __shared__ unsigned s_ticket, s_chunk;
     const int nbins = a.lp.nbins;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const double boxtokpc = a.lp.vbox / nbins / a.lp.velfac;
+    const double bintov_d = a.lp.vbox / nbins;
     Counters ct = {0, 0, 0, 0, 0};
     if constexpr (PREC == 1 && TAU)
         stage_voigt32(vtab);
+    const Bound32 bk(a.lp);
+    // dynamic shared memory: [accumulators lo, hi (smem_mode)] [pair staging]
+    Stage32 *stage = reinterpret_cast<Stage32 *>(smem + (a.smem_mode ? 2 * (size_t)nbins : 0));
 
     unsigned ticket = blockIdx.x;
     if (a.persistent) {
@@ -861,7 +992,10 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         double b = 0.0;
         for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
             const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
-            b += TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
+            if constexpr (TAU && PREC == 1)
+                b += tau_pair_bound32(bk, in);
+            else
+                b += TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
         }
         const double B = block_sum(b, red);
         if (threadIdx.x == 0)
@@ -878,26 +1012,22 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
             lo[j] = 0ull;
             hi[j] = 0ull;
         }
+        if (threadIdx.x == 0)
+            s_chunk = 0u;
         __syncthreads();
         const int S = (B > 0.0 && !s_bad) ? 124 - ilogb(B) : 0;
         // 2. deposit: warp per pair
-        if (!s_bad && B > 0.0) {
+        if constexpr (TAU && PREC == 1) {
+            if (!s_bad && B > 0.0)
+                deposit_pairs32<COUNT>(a, axis, e0, e1, S, lo, hi, &s_bad, stage + warp * a.chunk,
+                                       &s_chunk, vtab, bintov_d, lane, ct);
+        } else if (!s_bad && B > 0.0) {
             for (long long e = e0 + warp; e < e1; e += nwarps) {
                 const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
                 if constexpr (TAU) {
-                    if constexpr (PREC == 0) {
-                        Tau64 s;
-                        if (s.setup(a.lp, in))
-                            walk_tau<0, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
-                    } else {
-                        Tau32 s;
-                        if (s.setup(a.lp, in)) {
-                            if (s.careful)
-                                walk_tau_careful<COUNT>(a, in, S, lo, hi, &s_bad, lane, ct);
-                            else
-                                walk_tau<1, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
-                        }
-                    }
+                    Tau64 s;
+                    if (s.setup(a.lp, in))
+                        walk_tau<0, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
                 } else {
                     Colden c;
                     if (c.setup(a.lp, in, boxtokpc)) {
@@ -1139,7 +1269,7 @@ __global__ void __launch_bounds__(512) grad_kernel(GradArgs a)
                 gv = (float)v_;
                 gtmp = (float)t_;
             } else {
-                const int j0 = wrap_bin(s.zmax, nbins);
+                const int j0 = s.j0;
                 const float lane_f = (float)lane;
                 float ad = 0.f, av = 0.f, at = 0.f;
                 for (int dir = 0; dir < 2; dir++) {
@@ -1229,7 +1359,8 @@ int resident_ctas(int threads, size_t smem)
 
 }  // namespace
 
-int deposit_max_smem_bins()
+namespace {
+int max_smem_optin()
 {
     if (g_max_smem_optin < 0) {
         int dev = 0, v = 0;
@@ -1237,18 +1368,53 @@ int deposit_max_smem_bins()
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         g_max_smem_optin = v;
     }
-    // static shared memory of the kernel is < 1.5 KiB
-    return (g_max_smem_optin - 2048) / 16;
+    return g_max_smem_optin;
+}
+// static shared memory of the deposit kernel is < 1.5 KiB
+constexpr int STATIC_SMEM_RESERVE = 2048;
+}  // namespace
+
+size_t deposit_smem_bytes(const DepositLaunch &cfg, int nbins)
+{
+    return (cfg.smem_mode ? (size_t)16 * nbins : 0) +
+           (size_t)(cfg.threads / 32) * cfg.chunk * sizeof(Stage32);
 }
 
-int deposit_resident_ctas(int compute_tau, int precision, int threads, int nbins, int smem_mode)
+void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 {
-    const size_t smem = smem_mode ? (size_t)16 * nbins : 0;
+    const size_t cap = (size_t)(max_smem_optin() - STATIC_SMEM_RESERVE);
+    if (compute_tau && cfg.precision == 1) {
+        // staged pairs: 32 per warp, or 16 to keep the accumulators on chip
+        for (int chunk : {32, 16}) {
+            cfg.chunk = chunk;
+            cfg.smem_mode = 1;
+            if (deposit_smem_bytes(cfg, nbins) <= cap)
+                return;
+        }
+        cfg.chunk = 32;
+        cfg.smem_mode = 0;
+        return;
+    }
+    cfg.chunk = 0;
+    cfg.smem_mode = (size_t)16 * nbins <= cap;
+}
+
+int deposit_max_smem_bins(int compute_tau, int precision, int threads)
+{
+    const size_t stage = (compute_tau && precision == 1)
+                             ? (size_t)(threads / 32) * 16 * sizeof(Stage32) : 0;
+    return (int)(((size_t)(max_smem_optin() - STATIC_SMEM_RESERVE) - stage) / 16);
+}
+
+int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins)
+{
+    const size_t smem = deposit_smem_bytes(cfg, nbins);
+    const int threads = cfg.threads;
     if (compute_tau)
-        return precision ? resident_ctas<true, 1, false>(threads, smem)
-                         : resident_ctas<true, 0, false>(threads, smem);
-    return precision ? resident_ctas<false, 1, false>(threads, smem)
-                     : resident_ctas<false, 0, false>(threads, smem);
+        return cfg.precision ? resident_ctas<true, 1, false>(threads, smem)
+                             : resident_ctas<true, 0, false>(threads, smem);
+    return cfg.precision ? resident_ctas<false, 1, false>(threads, smem)
+                         : resident_ctas<false, 0, false>(threads, smem);
 }
 
 void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
@@ -1275,7 +1441,8 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
     a.counters = counters;
     a.smem_mode = cfg.smem_mode;
     a.persistent = cfg.persistent;
-    const size_t smem = cfg.smem_mode ? (size_t)16 * lp.nbins : 0;
+    a.chunk = cfg.chunk;
+    const size_t smem = deposit_smem_bytes(cfg, lp.nbins);
     const int grid = cfg.persistent ? cfg.grid : nlos;
     const int threads = cfg.threads;
     const bool count = counters != nullptr;

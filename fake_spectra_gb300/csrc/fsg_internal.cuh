@@ -151,6 +151,7 @@ struct DepositLaunch {
     int persistent;          // 1: grid of resident CTAs draining a ticket queue
     int grid;                // persistent grid size (CTAs)
     int smem_mode;           // 1: per-sightline shared-memory accumulators
+    int chunk;               // pairs staged per warp (FP32 tau form), else 0
 };
 
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
@@ -163,8 +164,13 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
                     unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
                     unsigned long long *gacc, unsigned long long *counters,
                     const DepositLaunch &cfg, cudaStream_t s);
+// Chooses cfg.smem_mode and cfg.chunk (cfg.precision and cfg.threads set):
+// shared-memory accumulators whenever they fit beside the pair staging area.
+void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins);
+// Dynamic shared memory of one deposit CTA.
+size_t deposit_smem_bytes(const DepositLaunch &cfg, int nbins);
 // CTAs of the deposit kernel that fit on one SM for this configuration.
-int deposit_resident_ctas(int compute_tau, int precision, int threads, int nbins, int smem_mode);
+int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins);
 // Plain FP64 atomics into out for the listed lines (non-finite propagation).
 void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Particles &p,
                              const PairLists &pl, const int *bad_lines, int n_bad, double *out,
@@ -176,7 +182,8 @@ void launch_deposit_fallback_dev(const LineParams &lp, const LineTables &t, cons
                                  const PairLists &pl, const int *bad_lines, const int *n_bad_dev,
                                  int nlos, double *out, unsigned *dev_err, cudaStream_t s);
 
-int deposit_max_smem_bins();
+// Largest nbins whose accumulators fit in shared memory (smallest staging area).
+int deposit_max_smem_bins(int compute_tau, int precision, int threads);
 
 // Backward of the FP32 tau deposit: accumulates (+=) dL/d(dens), dL/dT and
 // dL/d(vel[3p+axis-1]) from dL/dtau (grad_tau, [L*nbins]).  Persistent grid.

@@ -149,10 +149,12 @@ extern "C" int fsg_particle_interpolate_noalloc(
     }
     if (nlos == 0 || nbins == 0)
         return FSG_OK;
-    if (nbins > deposit_max_smem_bins())
+    const int threads = precision == FSG_PREC_FP64 ? 256 : 512;
+    const int max_bins = deposit_max_smem_bins(compute_tau, precision, threads);
+    if (nbins > max_bins)
         return set_error(errbuf, errlen, FSG_ERR_VALUE,
                          "nbins = %d exceeds the no-allocation limit of %d pixels (accumulators "
-                         "must fit in shared memory)", nbins, deposit_max_smem_bins());
+                         "must fit in shared memory)", nbins, max_bins);
 
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     int dev = 0;
@@ -300,13 +302,12 @@ extern "C" int fsg_particle_interpolate_noalloc(
                                             gamma, fosc, amumass, tautail);
         DepositLaunch cfg{};
         cfg.precision = precision;
-        cfg.threads = precision == FSG_PREC_FP64 ? 256 : 512;
-        cfg.smem_mode = 1;
+        cfg.threads = threads;
+        deposit_plan(cfg, compute_tau, nbins);   // smem_mode = 1 within max_bins
         cfg.persistent = precision == FSG_PREC_FP32 ? 1 : 0;
         int sms = 0;
         NA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
-        const int per_sm =
-            std::max(1, deposit_resident_ctas(compute_tau, precision, cfg.threads, nbins, 1));
+        const int per_sm = std::max(1, deposit_resident_ctas(cfg, compute_tau, nbins));
         cfg.grid = std::min(nlos, sms * per_sm);
         PairLists pl{d_off, d_part, d_dr2};
         NA_CUDA(cudaMemsetAsync(d_ticket, 0, 4, s), "memset");
