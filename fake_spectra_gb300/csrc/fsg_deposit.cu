@@ -515,19 +515,6 @@ struct Tau32 {
         sub_dv = npoints > 1 ? __fdividef(bintov, (float)(npoints - 1)) * inv_b : 0.f;
     }
 
-    // Setup of one pair by every lane (the backward kernel).
-    __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
-    {
-        const double bintov_d = lp.vbox / lp.nbins;
-        Stage32 st;
-        float snod;
-        if (!stage32_setup(lp, in, bintov_d, st, &snod))
-            return false;
-        load(st, (float)bintov_d);
-        scale_nod = snod;
-        return true;
-    }
-
     __device__ __forceinline__ int bin0(int) const { return j0; }
 
     // Called by every lane of the warp (lanes past the window compute and
@@ -721,29 +708,6 @@ struct Colden {
         const double plow = (boxtokpc * (double)z - pos1);
         return dens * kern_frac<double>(kernel, plow, plow + boxtokpc, smooth, dr2, zrange);
     }
-
-    __device__ __forceinline__ float value32(long long z) const
-    {
-        const long long k = z - zlow;
-        // the first and the last two pixels may be clipped by the support: FP64
-        if (k == 0 || k >= kmax - 1)
-            return (float)value64(z);
-        if (kernel != SPH_CUBIC && kernel != SPH_QUINTIC)
-            return dens_f * ((float)(3. / 4. / PI_D) * box_f);
-        const bool cubic = (kernel == SPH_CUBIC);
-        const float dz = box_f * (1.f / NGRID);
-        const float l0 = fmaf((float)k, box_f, dL0);
-        const float r0 = fmaf((float)(kmax - k), box_f, dR0);
-        float total = 0.f;
-#pragma unroll
-        for (int i = 0; i <= NGRID; i++) {
-            const float d = fminf(fmaf((float)i, dz, l0), fmaf(-(float)i, dz, r0));
-            const float eps = fmaf(d * (two_zr - d), inv_h2, ch);
-            const float kv = spline_from_eps(cubic, eps);
-            total += (i == 0 || i == NGRID) ? 0.5f * kv : kv;
-        }
-        return dens_f * (dz * total);
-    }
 };
 
 __device__ __forceinline__ double colden_pair_bound(const LineParams &lp, const PairInput &in,
@@ -756,6 +720,81 @@ __device__ __forceinline__ double colden_pair_bound(const LineParams &lp, const 
     const double wraps = ceil(npix / lp.nbins);
     return fabs((double)in.dens) * kernel_max(lp.kernel) * fabs(boxtokpc) * 1.001 *
            (wraps > 1.0 ? wraps : 1.0);
+}
+
+// Per-pair constants of the FP32 column density (48 bytes), set up by one
+// lane per pair like Stage32: the three FP64 edge pixels (first, last two)
+// are evaluated here, lane-parallel, and the interior walks in FP32.
+constexpr int COL_SKIP = 1, COL_BAD = 2;   // no overlap; window beyond the limit
+
+struct __align__(16) StageCol32 {
+    int j0, kmax, flags;
+    float dens_f;
+    float e0, e1, e2;        // pixels k = 0, kmax - 1, kmax
+    float dL0;
+    float dR0, two_zr, inv_h2, ch;
+};
+static_assert(sizeof(StageCol32) == 48, "StageCol32 is three 16-byte words");
+
+__device__ __forceinline__ void stagecol32_setup(const LineParams &lp, const PairInput &in,
+                                                 double btk, StageCol32 &st)
+{
+    Colden c;
+    st.flags = 0;
+    if (!c.setup(lp, in, btk)) {
+        st.flags = COL_SKIP;
+        return;
+    }
+    if (!c.ok) {
+        st.flags = COL_BAD;
+        return;
+    }
+    st.j0 = wrap_bin(c.zlow, lp.nbins);
+    st.kmax = (int)c.kmax;
+    st.dens_f = c.dens_f;
+    st.e0 = (float)c.value64(c.zlow);
+    st.e1 = c.kmax >= 2 ? (float)c.value64(c.zlow + c.kmax - 1) : 0.f;
+    st.e2 = c.kmax >= 1 ? (float)c.value64(c.zhigh) : 0.f;
+    st.dL0 = c.dL0;
+    st.dR0 = c.dR0;
+    st.two_zr = c.two_zr;
+    st.inv_h2 = c.inv_h2;
+    st.ch = c.ch;
+}
+
+// Colden::value32 for an interior pixel 0 < k < kmax - 1 of a staged pair.
+__device__ __forceinline__ float colden_interior32(const StageCol32 &st, int kernel, float box_f,
+                                                   int k)
+{
+    if (kernel != SPH_CUBIC && kernel != SPH_QUINTIC)
+        return st.dens_f * ((float)(3. / 4. / PI_D) * box_f);
+    const bool cubic = (kernel == SPH_CUBIC);
+    const float dz = box_f * (1.f / NGRID);
+    const float l0 = fmaf((float)k, box_f, st.dL0);
+    const float r0 = fmaf((float)(st.kmax - k), box_f, st.dR0);
+    float total = 0.f;
+#pragma unroll
+    for (int i = 0; i <= NGRID; i++) {
+        const float d = fminf(fmaf((float)i, dz, l0), fmaf(-(float)i, dz, r0));
+        const float eps = fmaf(d * (st.two_zr - d), st.inv_h2, st.ch);
+        const float kv = spline_from_eps(cubic, eps);
+        total += (i == 0 || i == NGRID) ? 0.5f * kv : kv;
+    }
+    return st.dens_f * (dz * total);
+}
+
+// colden_pair_bound in FP32 with a 1e-3 margin: the window length is bounded
+// by 2 zrange / pixel + 3 pixels.
+__device__ __forceinline__ double colden_pair_bound32(const LineParams &lp, const PairInput &in,
+                                                      float btk_abs, float kfac)
+{
+    const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+    if (hh2 - in.dr2 <= 0)
+        return 0.0;
+    const float zr = sqrtf((float)(hh2 - in.dr2));
+    const float npix = 2.f * zr / btk_abs + 3.f;
+    const float wraps = fmaxf(1.f, ceilf(npix / (float)lp.nbins));
+    return (double)(fabsf(in.dens) * kfac * btk_abs * wraps);
 }
 
 // ------------------------------------------------------------ reductions
@@ -880,12 +919,10 @@ __device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &
     const int nbins = a.lp.nbins;
     const int j0 = wrap_bin(c.zlow, nbins);
     const int kmax = (int)c.kmax;   // < MAX_COLDEN_WINDOW
+    static_assert(PREC == 0, "the FP32 column density walks staged pairs");
     for (int k = lane; k <= kmax; k += 32) {
         const int j = (int)(((long long)j0 + k) % nbins);
-        if constexpr (PREC == 0)
-            accumulate<double>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
-        else
-            accumulate<float>(a, c.value32(c.zlow + k), j, S, lo, hi, bad);
+        accumulate<double>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
         if (COUNT)
             ct.pixels++;
     }
@@ -957,6 +994,68 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
     }
 }
 
+// FP32 column density: chunks of staged pairs as in deposit_pairs32.
+template <bool COUNT>
+__device__ __forceinline__ void deposit_pairs_col32(const DepositArgs &a, int axis,
+                                                    long long e0, long long e1, int S,
+                                                    unsigned long long *lo,
+                                                    unsigned long long *hi, int *bad,
+                                                    StageCol32 *sw, unsigned *s_chunk,
+                                                    double btk, int lane, Counters &ct)
+{
+    const int chunk = a.chunk, nbins = a.lp.nbins, kernel = a.lp.kernel;
+    const float box_f = (float)btk;
+    for (;;) {
+        unsigned c = 0;
+        if (lane == 0)
+            c = atomicAdd(s_chunk, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        const long long cb = e0 + (long long)c * chunk;
+        if (cb >= e1)
+            break;
+        const int n = (int)min((long long)chunk, e1 - cb);
+        if (lane < n) {
+            const PairInput in = load_pair(a.p, a.pl, cb + lane, axis, false, a.dev_err);
+            StageCol32 st;
+            stagecol32_setup(a.lp, in, btk, st);
+            sw[lane] = st;
+        }
+        __syncwarp();
+        for (int q = 0; q < n; q++) {
+            const StageCol32 st = sw[q];
+            if (st.flags == COL_SKIP)
+                continue;
+            if (st.flags == COL_BAD) {
+                if (lane == 0)
+                    atomicOr(a.dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
+                *bad = 1;
+                continue;
+            }
+            int j = st.j0 + lane;
+            while (j >= nbins)
+                j -= nbins;
+            for (int k = lane; k <= st.kmax; k += 32) {
+                float v;
+                if (k == 0)
+                    v = st.e0;
+                else if (k == st.kmax)
+                    v = st.e2;
+                else if (k == st.kmax - 1)
+                    v = st.e1;
+                else
+                    v = colden_interior32(st, kernel, box_f, k);
+                accumulate<float>(a, v, j, S, lo, hi, bad);
+                if (COUNT)
+                    ct.pixels++;
+                j += 32;
+                while (j >= nbins)
+                    j -= nbins;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 template <bool TAU, int PREC, bool COUNT>
 __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     deposit_kernel(DepositArgs a)
@@ -976,6 +1075,9 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     const Bound32 bk(a.lp);
     // dynamic shared memory: [accumulators lo, hi (smem_mode)] [pair staging]
     Stage32 *stage = reinterpret_cast<Stage32 *>(smem + (a.smem_mode ? 2 * (size_t)nbins : 0));
+    StageCol32 *stage_col = reinterpret_cast<StageCol32 *>(stage);
+    const float btk_abs = (float)fabs(boxtokpc);
+    const float col_kfac = (float)(kernel_max(a.lp.kernel) * 1.001);
 
     unsigned ticket = blockIdx.x;
     if (a.persistent) {
@@ -994,6 +1096,8 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
             const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
             if constexpr (TAU && PREC == 1)
                 b += tau_pair_bound32(bk, in);
+            else if constexpr (!TAU && PREC == 1)
+                b += colden_pair_bound32(a.lp, in, btk_abs, col_kfac);
             else
                 b += TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
         }
@@ -1021,6 +1125,11 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
             if (!s_bad && B > 0.0)
                 deposit_pairs32<COUNT>(a, axis, e0, e1, S, lo, hi, &s_bad, stage + warp * a.chunk,
                                        &s_chunk, vtab, bintov_d, lane, ct);
+        } else if constexpr (!TAU && PREC == 1) {
+            if (!s_bad && B > 0.0)
+                deposit_pairs_col32<COUNT>(a, axis, e0, e1, S, lo, hi, &s_bad,
+                                           stage_col + warp * a.chunk, &s_chunk, boxtokpc, lane,
+                                           ct);
         } else if (!s_bad && B > 0.0) {
             for (long long e = e0 + warp; e < e1; e += nwarps) {
                 const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
@@ -1238,14 +1347,83 @@ __device__ __noinline__ void grad_pair_careful(const GradArgs &a, const PairInpu
     }
 }
 
-__global__ void __launch_bounds__(512) grad_kernel(GradArgs a)
+// Staged pair of the backward kernel: the forward constants plus what the
+// gradient needs (96 bytes).
+struct __align__(16) StageGrad {
+    Stage32 s;
+    float scale_nod, temp;
+    int ip, pad;
+};
+constexpr int GRAD_THREADS = 512, GRAD_CHUNK = 32;
+constexpr size_t GRAD_SMEM = (size_t)(GRAD_THREADS / 32) * GRAD_CHUNK * sizeof(StageGrad);
+
+// One warp, one FP32-walk pair: dL/d(dens), dL/d(v_los), dL/dT summed over the
+// pair's window (all lanes hold the sums afterwards).
+__device__ __forceinline__ void grad_pair32(const Tau32 &s, const double *gt, int nbins,
+                                            float tautail, int lane, const float2 *vtab,
+                                            float &ad, float &av, float &at)
 {
+    const int half = nbins / 2;
+    const int j0 = s.j0;
+    const float lane_f = (float)lane;
+    ad = av = at = 0.f;
+    for (int dir = 0; dir < 2; dir++) {
+        float kf = dir == 0 ? lane_f : -1.0f - lane_f;
+        const float dkf = dir == 0 ? 32.0f : -32.0f;
+        for (int step = 0; step < half; step += 32, kf += dkf) {
+            const int k = step + lane;
+            const bool valid = k < half;
+            const int koff = dir == 0 ? k : -1 - k;
+            const float vlow_b = fmaf(kf, s.bintov, s.base0) * s.inv_b;
+            GradSums g;
+            if (s.npoints == 1) {
+                g = grad_node_sums(s, vlow_b + s.hbin_b, vtab);
+            } else {
+                g = grad_node_sums(s, vlow_b, vtab);
+                g.d *= 0.5f;
+                g.v *= 0.5f;
+                g.t *= 0.5f;
+                for (int i = 1; i < s.npoints - 1; ++i) {
+                    const GradSums h = grad_node_sums(s, fmaf((float)i, s.sub_dv, vlow_b), vtab);
+                    g.d += h.d;
+                    g.v += h.v;
+                    g.t += h.t;
+                }
+                const GradSums h = grad_node_sums(s, vlow_b + 2.f * s.hbin_b, vtab);
+                g.d += 0.5f * h.d;
+                g.v += 0.5f * h.v;
+                g.t += 0.5f * h.t;
+            }
+            const float tl = s.scale * g.d;
+            const unsigned m = __ballot_sync(0xffffffffu, valid && tl < tautail);
+            const int last = m ? (__ffs(m) - 1) : 31;
+            if (valid && lane <= last) {
+                const float gg = (float)gt[bin_from(j0, koff, nbins)];
+                ad = fmaf(gg, g.d, ad);
+                av = fmaf(gg, g.v, av);
+                at = fmaf(gg, g.t, at);
+            }
+            if (m)
+                break;
+        }
+    }
+}
+
+// Sightlines from a ticket queue; within a sightline the warps take chunks of
+// pairs from a shared counter, each lane sets up one pair of the chunk (the
+// forward's lane-parallel setup) and the warp walks them one after another.
+__global__ void __launch_bounds__(GRAD_THREADS) grad_kernel(GradArgs a)
+{
+    extern __shared__ __align__(16) unsigned char gsmem[];
     __shared__ float2 vtab[FSG_V32_N];
-    __shared__ unsigned s_ticket;
+    __shared__ unsigned s_ticket, s_chunk;
     stage_voigt32(vtab);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int nbins = a.lp.nbins, half = nbins / 2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nbins = a.lp.nbins;
     const float tautail = (float)a.lp.tautail;
+    const double bintov_d = a.lp.vbox / nbins;
+    const float bintov_f = (float)bintov_d;
+    StageGrad *sw = reinterpret_cast<StageGrad *>(gsmem) + warp * GRAD_CHUNK;
     if (threadIdx.x == 0)
         s_ticket = atomicAdd(a.ticket, 1u);
     __syncthreads();
@@ -1255,79 +1433,63 @@ __global__ void __launch_bounds__(512) grad_kernel(GradArgs a)
         const int axis = a.t.axis[line];
         const double *gt = a.grad_tau + (size_t)line * nbins;
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
-        for (long long e = e0 + warp; e < e1; e += nwarps) {
-            const PairInput in = load_pair(a.p, a.pl, e, axis, true, a.dev_err);
-            const int ip = a.pl.part[e];
-            Tau32 s;
-            if (!s.setup(a.lp, in))
-                continue;
-            float gd = 0.f, gv = 0.f, gtmp = 0.f;
-            if (s.careful) {
-                double d_, v_, t_;
-                grad_pair_careful(a, in, gt, lane, d_, v_, t_);
-                gd = (float)d_;
-                gv = (float)v_;
-                gtmp = (float)t_;
-            } else {
-                const int j0 = s.j0;
-                const float lane_f = (float)lane;
-                float ad = 0.f, av = 0.f, at = 0.f;
-                for (int dir = 0; dir < 2; dir++) {
-                    float kf = dir == 0 ? lane_f : -1.0f - lane_f;
-                    const float dkf = dir == 0 ? 32.0f : -32.0f;
-                    for (int step = 0; step < half; step += 32, kf += dkf) {
-                        const int k = step + lane;
-                        const bool valid = k < half;
-                        const int koff = dir == 0 ? k : -1 - k;
-                        const float vlow_b = fmaf(kf, s.bintov, s.base0) * s.inv_b;
-                        GradSums g;
-                        if (s.npoints == 1) {
-                            g = grad_node_sums(s, vlow_b + s.hbin_b, vtab);
-                        } else {
-                            g = grad_node_sums(s, vlow_b, vtab);
-                            g.d *= 0.5f;
-                            g.v *= 0.5f;
-                            g.t *= 0.5f;
-                            for (int i = 1; i < s.npoints - 1; ++i) {
-                                const GradSums h =
-                                    grad_node_sums(s, fmaf((float)i, s.sub_dv, vlow_b), vtab);
-                                g.d += h.d;
-                                g.v += h.v;
-                                g.t += h.t;
-                            }
-                            const GradSums h = grad_node_sums(s, vlow_b + 2.f * s.hbin_b, vtab);
-                            g.d += 0.5f * h.d;
-                            g.v += 0.5f * h.v;
-                            g.t += 0.5f * h.t;
-                        }
-                        const float tl = s.scale * g.d;
-                        const unsigned m = __ballot_sync(0xffffffffu, valid && tl < tautail);
-                        const int last = m ? (__ffs(m) - 1) : 31;
-                        if (valid && lane <= last) {
-                            const float gg = (float)gt[bin_from(j0, koff, nbins)];
-                            ad = fmaf(gg, g.d, ad);
-                            av = fmaf(gg, g.v, av);
-                            at = fmaf(gg, g.t, at);
-                        }
-                        if (m)
-                            break;
-                    }
+        if (threadIdx.x == 0)
+            s_chunk = 0u;
+        __syncthreads();
+        for (;;) {
+            unsigned c = 0;
+            if (lane == 0)
+                c = atomicAdd(&s_chunk, 1u);
+            c = __shfl_sync(0xffffffffu, c, 0);
+            const long long cb = e0 + (long long)c * GRAD_CHUNK;
+            if (cb >= e1)
+                break;
+            const int n = (int)min((long long)GRAD_CHUNK, e1 - cb);
+            if (lane < n) {
+                const PairInput in = load_pair(a.p, a.pl, cb + lane, axis, true, a.dev_err);
+                StageGrad g;
+                g.temp = in.temp;
+                g.ip = a.pl.part[cb + lane];
+                g.pad = 0;
+                if (!stage32_setup(a.lp, in, bintov_d, g.s, &g.scale_nod))
+                    g.s.flags = STAGE_SKIP;
+                sw[lane] = g;
+            }
+            __syncwarp();
+            for (int k = 0; k < n; k++) {
+                const StageGrad g = sw[k];
+                if (g.s.flags & STAGE_SKIP)
+                    continue;
+                float gd = 0.f, gv = 0.f, gtmp = 0.f;
+                if (g.s.flags & STAGE_CAREFUL) {
+                    const PairInput in = load_pair(a.p, a.pl, cb + k, axis, true, a.dev_err);
+                    double d_, v_, t_;
+                    grad_pair_careful(a, in, gt, lane, d_, v_, t_);
+                    gd = (float)d_;
+                    gv = (float)v_;
+                    gtmp = (float)t_;
+                } else {
+                    Tau32 s;
+                    s.load(g.s, bintov_f);
+                    float ad, av, at;
+                    grad_pair32(s, gt, nbins, tautail, lane, vtab, ad, av, at);
+                    gd = g.scale_nod * ad;
+                    gv = s.scale * s.inv_b * av;
+                    gtmp = -s.scale / (2.0f * g.temp) * at;
                 }
-                gd = s.scale_nod * ad;
-                gv = s.scale * s.inv_b * av;
-                gtmp = -s.scale / (2.0f * in.temp) * at;
-            }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                gd += __shfl_xor_sync(0xffffffffu, gd, o);
-                gv += __shfl_xor_sync(0xffffffffu, gv, o);
-                gtmp += __shfl_xor_sync(0xffffffffu, gtmp, o);
+                for (int o = 16; o > 0; o >>= 1) {
+                    gd += __shfl_xor_sync(0xffffffffu, gd, o);
+                    gv += __shfl_xor_sync(0xffffffffu, gv, o);
+                    gtmp += __shfl_xor_sync(0xffffffffu, gtmp, o);
+                }
+                if (lane == 0) {
+                    atomicAdd(&a.g_dens[g.ip], gd);
+                    atomicAdd(&a.g_temp[g.ip], gtmp);
+                    atomicAdd(&a.g_vel[3ll * g.ip + axis - 1], gv);
+                }
             }
-            if (lane == 0) {
-                atomicAdd(&a.g_dens[ip], gd);
-                atomicAdd(&a.g_temp[ip], gtmp);
-                atomicAdd(&a.g_vel[3ll * ip + axis - 1], gv);
-            }
+            __syncwarp();
         }
         __syncthreads();
         if (threadIdx.x == 0)
@@ -1374,21 +1536,30 @@ int max_smem_optin()
 constexpr int STATIC_SMEM_RESERVE = 2048;
 }  // namespace
 
-size_t deposit_smem_bytes(const DepositLaunch &cfg, int nbins)
+namespace {
+size_t stage_pair_bytes(int compute_tau, int precision)
+{
+    if (precision != 1)
+        return 0;
+    return compute_tau ? sizeof(Stage32) : sizeof(StageCol32);
+}
+}  // namespace
+
+size_t deposit_smem_bytes(const DepositLaunch &cfg, int compute_tau, int nbins)
 {
     return (cfg.smem_mode ? (size_t)16 * nbins : 0) +
-           (size_t)(cfg.threads / 32) * cfg.chunk * sizeof(Stage32);
+           (size_t)(cfg.threads / 32) * cfg.chunk * stage_pair_bytes(compute_tau, cfg.precision);
 }
 
 void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 {
     const size_t cap = (size_t)(max_smem_optin() - STATIC_SMEM_RESERVE);
-    if (compute_tau && cfg.precision == 1) {
+    if (cfg.precision == 1) {
         // staged pairs: 32 per warp, or 16 to keep the accumulators on chip
         for (int chunk : {32, 16}) {
             cfg.chunk = chunk;
             cfg.smem_mode = 1;
-            if (deposit_smem_bytes(cfg, nbins) <= cap)
+            if (deposit_smem_bytes(cfg, compute_tau, nbins) <= cap)
                 return;
         }
         cfg.chunk = 32;
@@ -1401,14 +1572,13 @@ void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 
 int deposit_max_smem_bins(int compute_tau, int precision, int threads)
 {
-    const size_t stage = (compute_tau && precision == 1)
-                             ? (size_t)(threads / 32) * 16 * sizeof(Stage32) : 0;
+    const size_t stage = (size_t)(threads / 32) * 16 * stage_pair_bytes(compute_tau, precision);
     return (int)(((size_t)(max_smem_optin() - STATIC_SMEM_RESERVE) - stage) / 16);
 }
 
 int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins)
 {
-    const size_t smem = deposit_smem_bytes(cfg, nbins);
+    const size_t smem = deposit_smem_bytes(cfg, compute_tau, nbins);
     const int threads = cfg.threads;
     if (compute_tau)
         return cfg.precision ? resident_ctas<true, 1, false>(threads, smem)
@@ -1442,7 +1612,7 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
     a.smem_mode = cfg.smem_mode;
     a.persistent = cfg.persistent;
     a.chunk = cfg.chunk;
-    const size_t smem = deposit_smem_bytes(cfg, lp.nbins);
+    const size_t smem = deposit_smem_bytes(cfg, lp.compute_tau, lp.nbins);
     const int grid = cfg.persistent ? cfg.grid : nlos;
     const int threads = cfg.threads;
     const bool count = counters != nullptr;
@@ -1511,13 +1681,17 @@ void launch_tau_backward(const LineParams &lp, const LineTables &t, const Partic
     a.g_vel = g_vel;
     a.ticket = ticket;
     a.dev_err = dev_err;
-    grad_kernel<<<grid, 512, 0, s>>>(a);
+    cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)GRAD_SMEM);
+    grad_kernel<<<grid, GRAD_THREADS, GRAD_SMEM, s>>>(a);
 }
 
 int tau_backward_resident_ctas()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, grad_kernel, 512, 0);
+    cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)GRAD_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, grad_kernel, GRAD_THREADS, GRAD_SMEM);
     return n;
 }
 

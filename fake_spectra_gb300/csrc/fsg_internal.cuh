@@ -151,7 +151,7 @@ struct DepositLaunch {
     int persistent;          // 1: grid of resident CTAs draining a ticket queue
     int grid;                // persistent grid size (CTAs)
     int smem_mode;           // 1: per-sightline shared-memory accumulators
-    int chunk;               // pairs staged per warp (FP32 tau form), else 0
+    int chunk;               // pairs staged per warp (FP32 form), else 0
 };
 
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
@@ -168,7 +168,7 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
 // shared-memory accumulators whenever they fit beside the pair staging area.
 void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins);
 // Dynamic shared memory of one deposit CTA.
-size_t deposit_smem_bytes(const DepositLaunch &cfg, int nbins);
+size_t deposit_smem_bytes(const DepositLaunch &cfg, int compute_tau, int nbins);
 // CTAs of the deposit kernel that fit on one SM for this configuration.
 int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins);
 // Plain FP64 atomics into out for the listed lines (non-finite propagation).
