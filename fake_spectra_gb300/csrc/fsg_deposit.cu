@@ -175,19 +175,6 @@ __device__ __forceinline__ bool to_fixed(double c, int S, unsigned long long &lo
     return mant_to_fixed(m, e - 1075 + S, bits < 0, lo, hi, 53);
 }
 
-__device__ __forceinline__ bool to_fixed(float c, int S, unsigned long long &lo,
-                                         unsigned long long &hi)
-{
-    const int bits = __float_as_int(c);
-    unsigned long long m = (unsigned long long)(bits & 0x7FFFFF);
-    int e = (bits >> 23) & 0xFF;
-    if (e == 0)
-        e = 1;
-    else
-        m |= (1ull << 23);
-    return mant_to_fixed(m, e - 150 + S, bits < 0, lo, hi, 24);
-}
-
 __device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long long *hi, int j,
                                           unsigned long long l, unsigned long long h)
 {
@@ -203,6 +190,102 @@ __device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long 
 __device__ __forceinline__ double from_fixed(unsigned long long lo, unsigned long long hi, int S)
 {
     const double v = fma((double)(long long)hi, 18446744073709551616.0, (double)lo);
+    return scalbn(v, -S);
+}
+
+// ------------------------------------------------- split fixed point (FP32 form)
+// value * 2^S = hi * 2^32 + lo with lo in [0, 2^32).  The lo limbs and the
+// signed hi parts accumulate in two 64-bit words per pixel with no carry
+// between them (lo stays below 2^64 for fewer than 2^32 contributions), so each
+// add is a fire-and-forget atomic.  S puts the sightline bound B at 2^91, so hi
+// stays below 2^60.  The integer sums are exact: results do not depend on the
+// order of the adds.
+constexpr int SPLIT_TOP = 91;
+
+__device__ __forceinline__ void split_sign(bool neg, unsigned l32, unsigned long long h,
+                                           unsigned long long &lo, long long &hi)
+{
+    if (neg) {   // -(h 2^32 + l) = (-h - [l != 0]) 2^32 + (2^32 - l) mod 2^32
+        hi = -(long long)h - (l32 != 0u ? 1 : 0);
+        lo = (unsigned long long)(0u - l32);
+    } else {
+        hi = (long long)h;
+        lo = l32;
+    }
+}
+
+// Returns false if |v| 2^S >= 2^92 (round to nearest, ties away from zero).
+__device__ __forceinline__ bool split_from(float v, int S, unsigned long long &lo, long long &hi)
+{
+    const int bits = __float_as_int(v);
+    unsigned m = (unsigned)bits & 0x7FFFFFu;
+    int e = (bits >> 23) & 0xFF;
+    if (e == 0)
+        e = 1;
+    else
+        m |= 0x800000u;
+    const int p = e - 150 + S;   // |v| 2^S = m 2^p, m < 2^24
+    unsigned l32;
+    unsigned long long h;
+    if (p >= 32) {
+        if (p > 68)
+            return false;
+        l32 = 0u;
+        h = (unsigned long long)m << (p - 32);
+    } else if (p >= 0) {
+        const unsigned long long c = (unsigned long long)m << p;
+        l32 = (unsigned)c;
+        h = c >> 32;
+    } else {
+        l32 = (p < -25) ? 0u : (((m >> (-p - 1)) + 1u) >> 1);
+        h = 0;
+    }
+    split_sign(bits < 0, l32, h, lo, hi);
+    return true;
+}
+
+__device__ __forceinline__ bool split_from(double v, int S, unsigned long long &lo, long long &hi)
+{
+    const long long bits = __double_as_longlong(v);
+    unsigned long long m = (unsigned long long)bits & 0xFFFFFFFFFFFFFull;
+    int e = (int)((bits >> 52) & 0x7FF);
+    if (e == 0)
+        e = 1;
+    else
+        m |= (1ull << 52);
+    const int p = e - 1075 + S;   // |v| 2^S = m 2^p, m < 2^53
+    unsigned l32;
+    unsigned long long h;
+    if (p >= 32) {
+        if (p > 39)
+            return false;
+        l32 = 0u;
+        h = m << (p - 32);
+    } else if (p >= 0) {
+        l32 = (unsigned)(m << p);
+        h = p == 0 ? (m >> 32) : (m >> (32 - p));
+    } else {
+        const unsigned long long c = (p < -54) ? 0ull : (((m >> (-p - 1)) + 1ull) >> 1);
+        l32 = (unsigned)c;
+        h = c >> 32;
+    }
+    split_sign(bits < 0, l32, h, lo, hi);
+    return true;
+}
+
+__device__ __forceinline__ void split_add(unsigned long long *lo_acc, unsigned long long *hi_acc,
+                                          int j, unsigned long long lo, long long hi)
+{
+    if (lo)
+        atomicAdd(&lo_acc[j], lo);
+    if (hi)
+        atomicAdd(&hi_acc[j], (unsigned long long)hi);
+}
+
+__device__ __forceinline__ double from_split(unsigned long long lo, unsigned long long hi, int S)
+{
+    const long long h = (long long)hi + (long long)(lo >> 32);
+    const double v = fma((double)h, 4294967296.0, (double)(lo & 0xFFFFFFFFull));
     return scalbn(v, -S);
 }
 
@@ -483,6 +566,7 @@ struct Tau32 {
     float A[MP_R];              // multipole coefficients (far wing)
     float vmp;                  // |V| beyond which the multipole form holds
     float inv_b, base0, bintov, hbin_b, scale, scale_nod, sub_dv;
+    float vk, v0, vmid0;        // pixel k: V_low = k vk + v0, V_mid = k vk + vmid0
     float aa_f;
     int j0;
     int npoints;                 // 1: midpoint; else trapezoid points (uniform per pair)
@@ -506,10 +590,13 @@ struct Tau32 {
         w[3] = st.w[3];
 #pragma unroll
         for (int r = 0; r < MP_R; ++r)
-            A[r] = st.A[r];
+            A[r] = scale * st.A[r];   // inner() returns scaled sums
         vmp = st.vmp;
         bintov = bintov_f;
         hbin_b = 0.5f * bintov * inv_b;
+        vk = bintov * inv_b;
+        v0 = base0 * inv_b;
+        vmid0 = v0 + hbin_b;
         npoints = st.flags & STAGE_NP;
         careful = (st.flags & STAGE_CAREFUL) != 0;
         sub_dv = npoints > 1 ? __fdividef(bintov, (float)(npoints - 1)) * inv_b : 0.f;
@@ -517,8 +604,9 @@ struct Tau32 {
 
     __device__ __forceinline__ int bin0(int) const { return j0; }
 
-    // Called by every lane of the warp (lanes past the window compute and
-    // discard), so the warp votes below see a converged warp.
+    // scale x the node sum at V (velocity offset / b).  Called by every lane
+    // of the warp (lanes past the window compute and discard), so the warp
+    // votes below see a converged warp.
     template <bool COUNT>
     __device__ __forceinline__ float inner(float V, const float2 *tab, Counters &ct) const
     {
@@ -534,6 +622,12 @@ struct Tau32 {
             }
             return sm * W;
         }
+        return scale * inner_nodes<COUNT>(V, tab, ct);
+    }
+
+    template <bool COUNT>
+    __device__ __forceinline__ float inner_nodes(float V, const float2 *tab, Counters &ct) const
+    {
         float total = 0.f;
         float u[NODES];
         bool wing = true, core = true;
@@ -576,15 +670,14 @@ struct Tau32 {
     __device__ __forceinline__ float taulast(float kf, unsigned *dev_err, const float2 *tab,
                                              Counters &ct) const
     {
-        const float k = kf;
-        const float vlow_b = fmaf(k, bintov, base0) * inv_b;   // (v_low - v_particle) / b
         if (npoints == 1)
-            return scale * inner<COUNT>(vlow_b + hbin_b, tab, ct);
+            return inner<COUNT>(fmaf(kf, vk, vmid0), tab, ct);
+        const float vlow_b = fmaf(kf, vk, v0);   // (v_low - v_particle) / b
         float total = 0.5f * inner<COUNT>(vlow_b, tab, ct);
         for (int i = 1; i < npoints - 1; ++i)
             total += inner<COUNT>(fmaf((float)i, sub_dv, vlow_b), tab, ct);
         total += 0.5f * inner<COUNT>(vlow_b + 2.f * hbin_b, tab, ct);
-        return scale * total;
+        return total;
     }
 };
 
@@ -834,7 +927,8 @@ struct DepositArgs {
     int chunk;                      // pairs staged per warp (FP32 tau form)
 };
 
-template <class R>
+// FMT 0: 128-bit fixed point with carries (FP64 form); 1: split (FP32 form).
+template <class R, int FMT>
 __device__ __forceinline__ void accumulate(const DepositArgs &a, R v, int j, int S,
                                            unsigned long long *lo, unsigned long long *hi,
                                            int *bad)
@@ -843,11 +937,20 @@ __device__ __forceinline__ void accumulate(const DepositArgs &a, R v, int j, int
         *bad = 1;
         return;
     }
-    unsigned long long l, h;
-    if (to_fixed(v, S, l, h))
-        fixed_add(lo, hi, j, l, h);
-    else
-        atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+    if constexpr (FMT == 0) {
+        unsigned long long l, h;
+        if (to_fixed(v, S, l, h))
+            fixed_add(lo, hi, j, l, h);
+        else
+            atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+    } else {
+        unsigned long long l;
+        long long h;
+        if (split_from(v, S, l, h))
+            split_add(lo, hi, j, l, h);
+        else
+            atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+    }
 }
 
 // bin of pixel zmax + koff from j0 = bin of zmax, |koff| <= nbins
@@ -864,7 +967,7 @@ __device__ __forceinline__ int bin_from(int j0, int koff, int nbins)
 // Walk one tau pair with the whole warp: 32 consecutive pixels per step.
 // Pixel offsets from zmax and bins are int32; the FP32 form compares its float
 // contribution with tautail in float, so no FP64 work is done per pixel.
-template <int PREC, bool COUNT, class P>
+template <int PREC, bool COUNT, int FMT, class P>
 __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S,
                                          unsigned long long *lo, unsigned long long *hi,
                                          int *bad, int lane, const float2 *tab, Counters &ct)
@@ -896,7 +999,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
             const unsigned m = __ballot_sync(0xffffffffu, stop);
             const int last = m ? (__ffs(m) - 1) : 31;
             if (valid && lane <= last) {
-                accumulate<R>(a, tl, bin_from(j0, koff, nbins), S, lo, hi, bad);
+                accumulate<R, FMT>(a, tl, bin_from(j0, koff, nbins), S, lo, hi, bad);
                 if (COUNT) {
                     ct.a += c1.a;
                     ct.b += c1.b;
@@ -922,7 +1025,7 @@ __device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &
     static_assert(PREC == 0, "the FP32 column density walks staged pairs");
     for (int k = lane; k <= kmax; k += 32) {
         const int j = (int)(((long long)j0 + k) % nbins);
-        accumulate<double>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
+        accumulate<double, 0>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
         if (COUNT)
             ct.pixels++;
     }
@@ -939,7 +1042,7 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
     if (!s.setup(a.lp, in))
         return;
     Counters c = {0, 0, 0, 0, 0};
-    walk_tau<0, COUNT>(a, s, S, lo, hi, bad, lane, nullptr, c);
+    walk_tau<0, COUNT, 1>(a, s, S, lo, hi, bad, lane, nullptr, c);
     if (COUNT) {
         ct.c += c.a + c.b + c.c;
         ct.pixels += c.pixels;
@@ -988,7 +1091,7 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
             }
             Tau32 s;
             s.load(st, bintov_f);
-            walk_tau<1, COUNT>(a, s, S, lo, hi, bad, lane, vtab, ct);
+            walk_tau<1, COUNT, 1>(a, s, S, lo, hi, bad, lane, vtab, ct);
         }
         __syncwarp();
     }
@@ -1044,7 +1147,7 @@ __device__ __forceinline__ void deposit_pairs_col32(const DepositArgs &a, int ax
                     v = st.e1;
                 else
                     v = colden_interior32(st, kernel, box_f, k);
-                accumulate<float>(a, v, j, S, lo, hi, bad);
+                accumulate<float, 1>(a, v, j, S, lo, hi, bad);
                 if (COUNT)
                     ct.pixels++;
                 j += 32;
@@ -1119,7 +1222,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         if (threadIdx.x == 0)
             s_chunk = 0u;
         __syncthreads();
-        const int S = (B > 0.0 && !s_bad) ? 124 - ilogb(B) : 0;
+        const int S = (B > 0.0 && !s_bad) ? (PREC == 0 ? 124 : SPLIT_TOP) - ilogb(B) : 0;
         // 2. deposit: warp per pair
         if constexpr (TAU && PREC == 1) {
             if (!s_bad && B > 0.0)
@@ -1136,7 +1239,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
                 if constexpr (TAU) {
                     Tau64 s;
                     if (s.setup(a.lp, in))
-                        walk_tau<0, COUNT>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
+                        walk_tau<0, COUNT, 0>(a, s, S, lo, hi, &s_bad, lane, vtab, ct);
                 } else {
                     Colden c;
                     if (c.setup(a.lp, in, boxtokpc)) {
@@ -1159,7 +1262,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         } else if (B > 0.0) {
             double *row = a.out + (size_t)line * nbins;
             for (int j = threadIdx.x; j < nbins; j += blockDim.x)
-                row[j] = from_fixed(lo[j], hi[j], S);
+                row[j] = PREC == 0 ? from_fixed(lo[j], hi[j], S) : from_split(lo[j], hi[j], S);
         }
         if (!a.persistent)
             break;
