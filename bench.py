@@ -39,10 +39,16 @@ sys.path.insert(0, ROOT)
 BASELINE_METRIC = ("Ly-α tau pixels/s, tuned FP32 vs plain FP64 GPU at max|ΔF|≤1e-4; "
                    "fwd+bwd ms")
 
-# Flops executed per Voigt-profile evaluation, counted once from the source of
-# each branch (fsg_voigt.cuh, fsg_deposit.cu) including the node sum of
-# tau_kern_inner; FMA = 2 flops, MUFU ops = 1.  Wing evaluations summed by the
-# multipole form cost 20 flops per pixel (7 evaluations): 20/7 each.
+# Algorithmic work unit of the roofline: one profile evaluation of the
+# reference's 7-node line-of-sight sum under its window rule, counted exactly by
+# the counting variant of the deposit kernel, at a frozen F_EVAL flops per
+# evaluation: the cheapest complete FP32 evaluation (asymptotic branch, 15 FMA
+# + 1 reciprocal, and the weighted add of the node sum; FMA = 2 flops).
+F_EVAL = 32
+# Flops executed per evaluation by each branch, counted once from the source
+# (fsg_voigt.cuh, fsg_deposit.cu), for the executed-flop figure beside it.  Wing
+# evaluations summed by the far-wing multipole form cost 20 flops per pixel
+# (7 evaluations): 20/7 each.
 FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
@@ -268,11 +274,15 @@ def main():
     step("fp32", o=torch.empty_like(out), count=True)
     cnt = ctx.stats()
     mp = cnt["evals_wing_multipole"]
-    flops = (cnt["evals_core"] * FLOPS_FP32["core"] + (cnt["evals_wing"] - mp) * FLOPS_FP32["wing"]
-             + cnt["evals_other"] * FLOPS_FP32["other"] + mp * FLOPS_FP32["multipole"])
+    evals = cnt["evals_core"] + cnt["evals_wing"] + cnt["evals_other"]
+    executed = (cnt["evals_core"] * FLOPS_FP32["core"]
+                + (cnt["evals_wing"] - mp) * FLOPS_FP32["wing"]
+                + cnt["evals_other"] * FLOPS_FP32["other"] + mp * FLOPS_FP32["multipole"])
     dep_mean = sum(dep_ms) / len(dep_ms)
     peak32 = _lib.fma_peak_tflops("fp32")
-    achieved = flops / (dep_mean * 1e-3) / 1e12
+    achieved = evals * F_EVAL / (dep_mean * 1e-3) / 1e12
+    achieved_exec = executed / (dep_mean * 1e-3) / 1e12
+    peak64 = _lib.fma_peak_tflops("fp64")
     res = {
         "metric": BASELINE_METRIC, "value": value, "unit": "pixels/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -291,12 +301,16 @@ def main():
                      "frac": achieved / peak32,
                      "peak_source": "measured: libfsg FMA-chain microbenchmark (MEASURED_PEAKS.json "
                                     "has no FP32 figure)",
-                     "work": {"evals_core": cnt["evals_core"], "evals_wing": cnt["evals_wing"],
+                     "work": {"unit": "reference profile evaluations (7 per pixel sample)",
+                              "evals": evals, "flops_per_eval": F_EVAL,
+                              "evals_core": cnt["evals_core"], "evals_wing": cnt["evals_wing"],
                               "evals_wing_multipole": mp,
                               "evals_other": cnt["evals_other"], "pixels": cnt["pixels"],
-                              "flops_per_eval": FLOPS_FP32,
-                              "algorithmic_evals_per_s": (cnt["evals_core"] + cnt["evals_wing"]
-                                                          + cnt["evals_other"]) / (dep_mean * 1e-3)},
+                              "launches_timed": 1,
+                              "deposit_ms_per_launch": dep_mean},
+                     "executed": {"flops_per_eval_by_branch": FLOPS_FP32,
+                                  "achieved": achieved_exec, "frac": achieved_exec / peak32},
+                     "peak_fp64": peak64,
                      "traffic": None},
     }
 
