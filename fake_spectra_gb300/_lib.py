@@ -36,6 +36,13 @@ EXPORTS = (
     "fsg_build_pairs_device",
     "fsg_copy_pairs",
     "fsg_particle_interpolate_noalloc",
+    "fsg_near_lines",
+    "fsg_near_lines_device",
+    "fsg_rescale_mean_flux",
+    "fsg_mean_flux_scale_device",
+    "fsg_mean_flux_device",
+    "fsg_flux_histogram_device",
+    "fsg_flux_power_device",
 )
 
 _c_int = ctypes.c_int
@@ -128,6 +135,20 @@ def load(path=None):
         L.fsg_particle_interpolate_noalloc.argtypes = ([_c_int, _c_int, _c_int] + [_c_d] * 8 +
                                                        [_p] * 5 + [_c_i64, _p, _p, _c_i32, _p,
                                                                    _c_int, _p, _p, _c_size])
+        L.fsg_near_lines.argtypes = [_c_d, _p, _p, _c_i64, _p, _p, _c_i32, _p,
+                                     ctypes.POINTER(_c_i64), _p, _c_size]
+        L.fsg_near_lines_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32, _p,
+                                            ctypes.POINTER(_c_i64), _p, _c_size]
+        L.fsg_rescale_mean_flux.argtypes = [_p, _c_i64, _c_d, _c_d, _c_d, ctypes.POINTER(_c_d),
+                                            _p, _c_size]
+        L.fsg_mean_flux_scale_device.argtypes = [_p, _p, _c_i64, _c_d, _c_d, _c_d,
+                                                 ctypes.POINTER(_c_d), _p, _c_size]
+        L.fsg_mean_flux_device.argtypes = [_p, _p, _c_i64, _c_d, ctypes.POINTER(_c_d), _p,
+                                           _c_size]
+        L.fsg_flux_histogram_device.argtypes = [_p, _p, _c_i64, _c_d, _p, _c_int, _p, _p,
+                                                _c_size]
+        L.fsg_flux_power_device.argtypes = [_p, _p, _c_i64, _c_i64, _c_d, _c_d, _c_d, _p, _p,
+                                            _c_size]
         _lib = L
         return L
 

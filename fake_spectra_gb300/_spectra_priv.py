@@ -1,5 +1,12 @@
 """Drop-in replacement for the reference extension module ``fake_spectra._spectra_priv``.
 
+``_near_lines`` keeps the reference's arguments, checks and result
+(py_module.cpp:25-99, Py_near_lines): the ascending int32 indices of the
+particles within their smoothing length of any sightline.
+
+``_rescale_mean_flux`` (py_module.cpp:262-282, Py_mean_flux) returns the
+Newton-Raphson scale of tau that gives the desired mean flux.
+
 ``_Particle_Interpolate`` keeps the reference's positional arguments, argument
 checks, exception classes and return value (py_module.cpp:103-233,
 Py_Particle_Interpolation): a new float64 array of shape (NumLos, nbins)
@@ -112,3 +119,69 @@ def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1):
                                     512)
     _lib.raise_for(rc, eb.value.decode(errors="replace"))
     return out
+
+
+def _near_lines(*args):
+    """Indices of the particles near any sightline; see the module docstring."""
+    if len(args) != 5:
+        raise TypeError("_near_lines takes (box, pos, hh, axis, cofm)")
+    box = _as_float(args[0])
+    pos, hh, axis, cofm = (_to_numpy(a) for a in args[1:5])
+    # the checks of py_module.cpp:36-54, in the same order and classes
+    if cofm.ndim < 2 or axis.ndim < 1:
+        raise ValueError("cofm must have dimensions (np.size(axis),3) \n")
+    if cofm.shape[0] != axis.shape[0] or cofm.shape[1] != 3:
+        raise ValueError("cofm must have dimensions (np.size(axis),3) \n")
+    if cofm.dtype != np.float64 or axis.dtype != np.int32:
+        raise ValueError("cofm must have 64-bit float type and axis must be a 32-bit integer\n")
+    if pos.dtype != np.float32 or hh.dtype != np.float32:
+        raise TypeError("pos and h must have 32-bit float type\n")
+    npart = pos.shape[0] if pos.ndim >= 1 else 0
+    if pos.ndim != 2 or pos.shape[1] != 3:
+        raise ValueError("pos must have dimensions (Npart, 3)\n")
+    if hh.ndim < 1 or hh.shape[0] < npart:
+        raise ValueError("h must have at least Npart entries\n")
+    pos = np.ascontiguousarray(pos)
+    hh = np.ascontiguousarray(hh)
+    axis = np.ascontiguousarray(axis)
+    cofm = np.ascontiguousarray(cofm)
+    nlos = int(axis.shape[0])
+    out = np.empty(max(npart, 1), dtype=np.int32)
+    if npart == 0 or nlos == 0:
+        return out[:0].copy()
+    n = ctypes.c_int64(0)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_near_lines(box, _ptr(pos), _ptr(hh), npart, _ptr(axis), _ptr(cofm), nlos,
+                          _ptr(out), ctypes.byref(n), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return out[:n.value].copy()
+
+
+_MF_MSG = ("Incorrect arguments: use tau (array), mean_flux_desired (double), nbins (int), "
+           "tol (double), thresh (double)\n")
+
+
+def _rescale_mean_flux(*args):
+    """Scale factor of tau with mean(exp(-scale tau)) = mean_flux_desired."""
+    if len(args) != 5 or not isinstance(args[0], np.ndarray):
+        raise AttributeError(_MF_MSG)
+    tau = args[0]
+    try:
+        mfd = float(args[1])
+        nbins = int(args[2].__index__()) if not isinstance(args[2], (int, np.integer)) \
+            else int(args[2])
+        tol, thresh = float(args[3]), float(args[4])
+    except Exception:
+        raise AttributeError(_MF_MSG) from None
+    if tau.dtype != np.float64:
+        raise TypeError("Optical depth must have 64-bit float type\n")
+    tau = np.ascontiguousarray(tau).reshape(-1)
+    if nbins < 0 or nbins > tau.size:
+        raise ValueError("nbins must be between 0 and the size of tau\n")
+    out = ctypes.c_double(0.0)
+    eb = _lib.errbuf()
+    rc = _lib.load().fsg_rescale_mean_flux(_ptr(tau), nbins, mfd, tol, thresh,
+                                           ctypes.byref(out), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return out.value

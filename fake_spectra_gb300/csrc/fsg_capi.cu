@@ -9,6 +9,8 @@
 //   3. deposit: sightlines ordered by descending pair count; one kernel;
 //      sightlines with non-finite contributions re-run by the fallback kernel.
 #include "fsg.h"
+#include <cufft.h>
+
 #include "fsg_internal.cuh"
 
 #include <algorithm>
@@ -76,6 +78,8 @@ struct fsg_context {
     DevBuf line_count, cursor, off, part, dr2, line_order;   // pair lists
     DevBuf ticket, bad, nbad, err, gacc, counters;           // deposit bookkeeping
     DevBuf skey, sperm, shist, sstart, ssums;                // particle ordering
+    DevBuf flag, tcount, tstart, tsums, idx;                 // _near_lines
+    DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // host mirrors
     std::vector<long long> h_off;
@@ -110,7 +114,9 @@ struct fsg_context {
                           &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
                           &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
-                          &skey, &sperm, &shist, &sstart, &ssums};
+                          &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
+                          &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
+                          &ffft, &fpower};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -227,24 +233,29 @@ void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int n
 }
 
 // 2. pair search
+// spatial order of the particles (counting sort by 3-D cell); null when n = 0
+int *order_particles(fsg_context *c, const Particles &p)
+{
+    if (p.n <= 0)
+        return nullptr;
+    const int G = sort_grid_side(p.n);
+    const size_t M = (size_t)G * G * G;
+    auto *key = (unsigned *)c->ensure(c->skey, sizeof(unsigned) * p.n);
+    int *perm = (int *)c->ensure(c->sperm, sizeof(int) * p.n);
+    auto *hist = (unsigned *)c->ensure(c->shist, sizeof(unsigned) * M);
+    auto *start = (unsigned *)c->ensure(c->sstart, sizeof(unsigned) * M);
+    auto *sums = (unsigned *)c->ensure(c->ssums, sizeof(unsigned) * (M / 2048 + 2));
+    launch_particle_order(p, c->tables.box, G, key, hist, start, sums, perm, c->stream);
+    c->stats.gpu_launches += 5;
+    cuda_check(cudaGetLastError(), "particle order launch");
+    return perm;
+}
+
 void search_pairs(fsg_context *c, const Particles &p, int nlos)
 {
     cudaStream_t s = c->stream;
     cuda_check(cudaEventRecord(c->ev[0], s), "event");
-    // spatial order of the particles (counting sort by 3-D cell)
-    int *perm = nullptr;
-    if (p.n > 0) {
-        const int G = sort_grid_side(p.n);
-        const size_t M = (size_t)G * G * G;
-        auto *key = (unsigned *)c->ensure(c->skey, sizeof(unsigned) * p.n);
-        perm = (int *)c->ensure(c->sperm, sizeof(int) * p.n);
-        auto *hist = (unsigned *)c->ensure(c->shist, sizeof(unsigned) * M);
-        auto *start = (unsigned *)c->ensure(c->sstart, sizeof(unsigned) * M);
-        auto *sums = (unsigned *)c->ensure(c->ssums, sizeof(unsigned) * (M / 2048 + 2));
-        launch_particle_order(p, c->tables.box, G, key, hist, start, sums, perm, s);
-        c->stats.gpu_launches += 5;
-        cuda_check(cudaGetLastError(), "particle order launch");
-    }
+    int *perm = order_particles(c, p);
     auto *cnt = (unsigned long long *)c->ensure(c->line_count, sizeof(unsigned long long) * nlos);
     cuda_check(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * nlos, s), "memset");
     launch_count_pairs(c->tables, p, perm, cnt, nullptr, s);
@@ -294,6 +305,79 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     if (h_err)
         fail(FSG_ERR_DEVICE, "pair search reported device error bits 0x%x (%s)", h_err,
              deverr_text(h_err).c_str());
+}
+
+// _near_lines (py_module.cpp:25-99): ascending indices of the particles within
+// their smoothing length of any sightline, written to out (device, capacity
+// p.n); returns their number.
+long long near_lines(fsg_context *c, const Particles &p, int *out)
+{
+    cudaStream_t s = c->stream;
+    if (p.n <= 0 || c->nlos <= 0)
+        return 0;
+    int *perm = order_particles(c, p);
+    auto *flag = (unsigned char *)c->ensure(c->flag, (size_t)p.n);
+    launch_flag_near(c->tables, p, perm, flag, s);
+    const long long nt = flag_tiles(p.n);
+    if (nt > 2048LL * 2048LL)
+        fail(FSG_ERR_VALUE, "too many particles for the near-lines compaction");
+    auto *tcount = (unsigned *)c->ensure(c->tcount, sizeof(unsigned) * nt);
+    auto *tstart = (unsigned *)c->ensure(c->tstart, sizeof(unsigned) * nt);
+    auto *tsums = (unsigned *)c->ensure(c->tsums, sizeof(unsigned) * (nt / 2048 + 2));
+    launch_flag_count(flag, p.n, tcount, s);
+    launch_exclusive_scan(tcount, tstart, tsums, (int)nt, s);
+    launch_flag_scatter(flag, p.n, tstart, out, s);
+    c->stats.gpu_launches += 6;
+    cuda_check(cudaGetLastError(), "near-lines launch");
+    unsigned last_start = 0, last_count = 0;
+    cuda_check(cudaMemcpyAsync(&last_start, tstart + (nt - 1), sizeof(unsigned),
+                               cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaMemcpyAsync(&last_count, tcount + (nt - 1), sizeof(unsigned),
+                               cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "near lines");
+    return (long long)last_start + last_count;
+}
+
+// get_mean_flux_scale (py_module.cpp:235-260): Newton-Raphson on the scale of
+// tau until the mean of exp(-scale tau) over the pixels with tau <= thresh is
+// mean_flux_desired; the same update and stopping rule, sums on the device.
+double mean_flux_scale(fsg_context *c, const double *tau, long long n, double mfd, double tol,
+                       double thresh)
+{
+    cudaStream_t s = c->stream;
+    auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
+    auto *out = (double *)c->ensure(c->fout, sizeof(double) * 4);
+    double scale, newscale = 1.0;
+    int iterations = 0;
+    do {
+        scale = newscale;
+        double h[3];
+        launch_flux_moments(tau, n, scale, thresh, part, out, s);
+        c->stats.gpu_launches += 2;
+        cuda_check(cudaGetLastError(), "flux moments launch");
+        cuda_check(cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, s), "read");
+        cuda_check(cudaStreamSynchronize(s), "flux moments");
+        newscale = scale + (h[0] - mfd * h[2]) / h[1];
+        if (newscale <= 0)
+            newscale = 1e-10;
+        if (++iterations > 10000)
+            fail(FSG_ERR_VALUE, "mean-flux rescaling did not converge in 10000 iterations");
+    } while (fabs(newscale - scale) > tol * newscale);
+    return newscale;
+}
+
+double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale)
+{
+    cudaStream_t s = c->stream;
+    auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
+    auto *out = (double *)c->ensure(c->fout, sizeof(double) * 4);
+    launch_flux_sum(tau, n, scale, part, out, s);
+    c->stats.gpu_launches += 2;
+    cuda_check(cudaGetLastError(), "flux sum launch");
+    double h = 0.0;
+    cuda_check(cudaMemcpyAsync(&h, out, sizeof h, cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "flux sum");
+    return h / (double)n;
 }
 
 DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt);
@@ -525,6 +609,27 @@ void ctx_init(fsg_context *c, int device)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
 }
 
+// The per-device context of the host-pointer entry points (created on first
+// use; the caller holds g_default_mu).
+fsg_context *default_context()
+{
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64)
+        fail(FSG_ERR_VALUE, "device ordinal %d out of range", dev);
+    if (!g_default[dev]) {
+        auto *c = new fsg_context();
+        try {
+            ctx_init(c, dev);
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        g_default[dev] = c;
+    }
+    return g_default[dev];
+}
+
 void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, double box,
                      double velfac, double lambda, double gamma, double fosc, double amumass,
                      double tautail, const Particles &p, const int32_t *axis, const double *cofm,
@@ -651,23 +756,8 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
     (void)atime;
     try {
         validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
-        int dev = 0;
-        cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        if (dev < 0 || dev >= 64)
-            fail(FSG_ERR_VALUE, "device ordinal %d out of range", dev);
-        fsg_context *c;
         std::lock_guard<std::mutex> lock(g_default_mu);
-        if (!g_default[dev]) {
-            c = new fsg_context();
-            try {
-                ctx_init(c, dev);
-            } catch (...) {
-                delete c;
-                throw;
-            }
-            g_default[dev] = c;
-        }
-        c = g_default[dev];
+        fsg_context *c = default_context();
         cudaStream_t s = c->stream;
         const size_t n3 = sizeof(float) * 3 * (size_t)npart, n1 = sizeof(float) * (size_t)npart;
         auto up = [&](DevBuf &b, const void *src, size_t bytes) -> const float * {
@@ -816,6 +906,210 @@ int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const
         search_pairs(ctx, p, nlos);
         if (npairs)
             *npairs = ctx->npairs;
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_near_lines_device(fsg_context *ctx, double box, const float *pos, const float *h,
+                          int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
+                          int32_t *out, int64_t *nout, char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx || !nout)
+            fail(FSG_ERR_VALUE, "ctx and nout must not be NULL");
+        validate_common(0, SPH_CUBIC, box, npart, nlos, axis, cofm);
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        build_tables(ctx, axis, cofm, nlos, box);
+        Particles p{pos, nullptr, nullptr, nullptr, h, (long long)npart};
+        *nout = near_lines(ctx, p, out);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_near_lines(double box, const float *pos, const float *h, int64_t npart,
+                   const int32_t *axis, const double *cofm, int32_t nlos, int32_t *out,
+                   int64_t *nout, char *errbuf, size_t errlen)
+{
+    try {
+        if (!nout)
+            fail(FSG_ERR_VALUE, "nout must not be NULL");
+        validate_common(0, SPH_CUBIC, box, npart, nlos, axis, cofm);
+        std::lock_guard<std::mutex> lock(g_default_mu);
+        fsg_context *c = default_context();
+        cudaStream_t s = c->stream;
+        const size_t n3 = sizeof(float) * 3 * (size_t)npart, n1 = sizeof(float) * (size_t)npart;
+        auto *dpos = (float *)c->ensure(c->pos, n3);
+        auto *dh = (float *)c->ensure(c->hh, n1);
+        if (npart > 0) {
+            cuda_check(cudaMemcpyAsync(dpos, pos, n3, cudaMemcpyHostToDevice, s), "H2D");
+            cuda_check(cudaMemcpyAsync(dh, h, n1, cudaMemcpyHostToDevice, s), "H2D");
+        }
+        build_tables(c, axis, cofm, nlos, box);
+        Particles p{dpos, nullptr, nullptr, nullptr, dh, (long long)npart};
+        auto *didx = (int *)c->ensure(c->idx, sizeof(int) * (size_t)npart);
+        const long long n = near_lines(c, p, didx);
+        if (n > 0)
+            cuda_check(cudaMemcpyAsync(out, didx, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost,
+                                       s), "D2H");
+        cuda_check(cudaStreamSynchronize(s), "D2H");
+        *nout = n;
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_mean_flux_scale_device(fsg_context *ctx, const double *tau, int64_t n,
+                               double mean_flux_desired, double tol, double thresh, double *scale,
+                               char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx || !scale)
+            fail(FSG_ERR_VALUE, "ctx and scale must not be NULL");
+        if (n < 0)
+            fail(FSG_ERR_VALUE, "negative array length");
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        *scale = mean_flux_scale(ctx, tau, n, mean_flux_desired, tol, thresh);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_rescale_mean_flux(const double *tau, int64_t n, double mean_flux_desired, double tol,
+                          double thresh, double *scale, char *errbuf, size_t errlen)
+{
+    try {
+        if (!scale)
+            fail(FSG_ERR_VALUE, "scale must not be NULL");
+        if (n < 0)
+            fail(FSG_ERR_VALUE, "negative array length");
+        std::lock_guard<std::mutex> lock(g_default_mu);
+        fsg_context *c = default_context();
+        auto *d = (double *)c->ensure(c->ftau, sizeof(double) * (size_t)n);
+        if (n > 0)
+            cuda_check(cudaMemcpyAsync(d, tau, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                                       c->stream), "H2D");
+        *scale = mean_flux_scale(c, d, n, mean_flux_desired, tol, thresh);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_mean_flux_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
+                         double *mean, char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx || !mean)
+            fail(FSG_ERR_VALUE, "ctx and mean must not be NULL");
+        if (n <= 0)
+            fail(FSG_ERR_VALUE, "the mean flux of an empty array is undefined");
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        *mean = mean_flux_of(ctx, tau, n, scale);
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
+                              const double *edges, int nb, int64_t *counts, char *errbuf,
+                              size_t errlen)
+{
+    try {
+        if (!ctx || !edges || !counts)
+            fail(FSG_ERR_VALUE, "ctx, edges and counts must not be NULL");
+        if (n < 0 || nb < 1 || nb > 16384)
+            fail(FSG_ERR_VALUE, "need n >= 0 and 1 <= nbins <= 16384 (got %lld, %d)",
+                 (long long)n, nb);
+        for (int j = 0; j < nb; j++)
+            if (!(edges[j] < edges[j + 1]))
+                fail(FSG_ERR_VALUE, "bin edges must increase monotonically");
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        cudaStream_t s = ctx->stream;
+        auto *de = (double *)ctx->ensure(ctx->fedges, sizeof(double) * (nb + 1));
+        auto *dc = (unsigned long long *)ctx->ensure(ctx->fcounts, sizeof(long long) * nb);
+        cuda_check(cudaMemcpyAsync(de, edges, sizeof(double) * (nb + 1), cudaMemcpyHostToDevice,
+                                   s), "H2D");
+        cuda_check(cudaMemsetAsync(dc, 0, sizeof(long long) * nb, s), "memset");
+        if (n > 0) {
+            launch_flux_hist(tau, n, scale, de, nb, dc, s);
+            ctx->stats.gpu_launches++;
+            cuda_check(cudaGetLastError(), "flux histogram launch");
+        }
+        cuda_check(cudaMemcpyAsync(counts, dc, sizeof(long long) * nb, cudaMemcpyDeviceToHost, s),
+                   "D2H");
+        cuda_check(cudaStreamSynchronize(s), "flux histogram");
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, int64_t npix,
+                          double scale, double mean_flux, double vmax, double *power,
+                          char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx || !power)
+            fail(FSG_ERR_VALUE, "ctx and power must not be NULL");
+        if (nspec <= 0 || npix <= 0 || npix > (1 << 28))
+            fail(FSG_ERR_VALUE, "need nspec > 0 and 0 < npix <= 2^28 (got %lld, %lld)",
+                 (long long)nspec, (long long)npix);
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        cudaStream_t s = ctx->stream;
+        const int nk = (int)(npix / 2 + 1);
+        // rows per batched transform: about 256 MB of real input at a time
+        long long rows = (256ll << 20) / (8 * npix);
+        rows = rows < 1 ? 1 : (rows > nspec ? nspec : rows);
+        auto *dflux = (double *)ctx->ensure(ctx->fdflux, sizeof(double) * rows * npix);
+        auto *F = ctx->ensure(ctx->ffft, sizeof(cufftDoubleComplex) * rows * nk);
+        auto *dp = (double *)ctx->ensure(ctx->fpower, sizeof(double) * nk);
+        cuda_check(cudaMemsetAsync(dp, 0, sizeof(double) * nk, s), "memset");
+        auto plan_for = [&](int batch) {
+            cufftHandle plan;
+            int n1 = (int)npix;
+            if (cufftPlanMany(&plan, 1, &n1, nullptr, 1, (int)npix, nullptr, 1, nk, CUFFT_D2Z,
+                              batch) != CUFFT_SUCCESS)
+                fail(FSG_ERR_CUDA, "cufftPlanMany failed");
+            if (cufftSetStream(plan, s) != CUFFT_SUCCESS) {
+                cufftDestroy(plan);
+                fail(FSG_ERR_CUDA, "cufftSetStream failed");
+            }
+            return plan;
+        };
+        cufftHandle plan = plan_for((int)rows);
+        long long plan_rows = rows;
+        try {
+            for (long long r0 = 0; r0 < nspec; r0 += rows) {
+                const long long r = (r0 + rows <= nspec) ? rows : nspec - r0;
+                if (r != plan_rows) {
+                    cufftDestroy(plan);
+                    plan = plan_for((int)r);
+                    plan_rows = r;
+                }
+                launch_dflux(tau + r0 * npix, r * npix, scale, 1.0 / mean_flux, dflux, s);
+                if (cufftExecD2Z(plan, dflux, (cufftDoubleComplex *)F) != CUFFT_SUCCESS)
+                    fail(FSG_ERR_CUDA, "cufftExecD2Z failed");
+                launch_power_accumulate(F, (int)r, nk, (int)npix, vmax, dp, s);
+                ctx->stats.gpu_launches += 2;
+                cuda_check(cudaGetLastError(), "flux power launch");
+            }
+        } catch (...) {
+            cufftDestroy(plan);
+            throw;
+        }
+        cufftDestroy(plan);
+        cuda_check(cudaMemcpyAsync(power, dp, sizeof(double) * nk, cudaMemcpyDeviceToHost, s),
+                   "D2H");
+        cuda_check(cudaStreamSynchronize(s), "flux power");
+        for (int k = 0; k < nk; k++)
+            power[k] /= (double)nspec;
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);

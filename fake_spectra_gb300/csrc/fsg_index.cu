@@ -384,6 +384,89 @@ __global__ void cell_scatter_kernel(const unsigned *key, unsigned *cursor, int *
     }
 }
 
+// _near_lines (py_module.cpp:25-99): flag[i] = 1 when particle i is within
+// its smoothing length of any sightline (IndexTable::get_near_lines non-empty,
+// index_table.cpp:117-127), by the same predicate as the pair search.
+__global__ void flag_near_kernel(LineTables t, Particles p, const int *perm, unsigned char *flag)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < p.n; k += stride) {
+        const long long i = perm ? (long long)perm[k] : k;
+        float pos3[3], hh;
+        load_particle(p, i, pos3, &hh);
+        int found = 0;
+        for_each_pair(t, pos3, hh, [&](int, double) { found = 1; });
+        flag[i] = (unsigned char)found;
+    }
+}
+
+// Ordered compaction of the flags into ascending particle indices: each
+// 256-thread block owns a tile of FLAG_TILE particles, 16 consecutive ones per
+// thread; pass 1 counts the tile, the tile counts are scanned, pass 2 writes.
+constexpr int FLAG_THREADS = 256, FLAG_PER_THREAD = 16, FLAG_TILE = FLAG_THREADS * FLAG_PER_THREAD;
+
+__device__ __forceinline__ int thread_flag_count(const unsigned char *flag, long long n,
+                                                 long long first)
+{
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < FLAG_PER_THREAD; q++)
+        c += (first + q < n) ? (int)(flag[first + q] != 0) : 0;
+    return c;
+}
+
+__global__ void __launch_bounds__(FLAG_THREADS) flag_count_kernel(const unsigned char *flag,
+                                                                  long long n, unsigned *tile_count)
+{
+    __shared__ int red[FLAG_THREADS / 32];
+    const long long first = (long long)blockIdx.x * FLAG_TILE + (long long)threadIdx.x * FLAG_PER_THREAD;
+    int c = thread_flag_count(flag, n, first);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < FLAG_THREADS / 32; w++)
+            t += red[w];
+        tile_count[blockIdx.x] = (unsigned)t;
+    }
+}
+
+__global__ void __launch_bounds__(FLAG_THREADS) flag_scatter_kernel(const unsigned char *flag,
+                                                                    long long n,
+                                                                    const unsigned *tile_start,
+                                                                    int *out)
+{
+    __shared__ int wsum[FLAG_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long first = (long long)blockIdx.x * FLAG_TILE + (long long)threadIdx.x * FLAG_PER_THREAD;
+    const int c = thread_flag_count(flag, n, first);
+    // exclusive scan of the per-thread counts across the block
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+            incl += v;
+    }
+    if (lane == 31)
+        wsum[warp] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; w++)
+        base += wsum[w];
+    long long slot = (long long)tile_start[blockIdx.x] + base + (incl - c);
+#pragma unroll
+    for (int q = 0; q < FLAG_PER_THREAD; q++) {
+        const long long i = first + q;
+        if (i < n && flag[i])
+            out[slot++] = (int)i;
+    }
+}
+
 __global__ void check_emit_kernel(const unsigned long long *line_count,
                                   const unsigned long long *cursor, int nlos, unsigned *dev_err)
 {
@@ -430,6 +513,43 @@ void launch_check_emit(const unsigned long long *line_count, const unsigned long
     if (nlos <= 0)
         return;
     check_emit_kernel<<<(nlos + 255) / 256, 256, 0, s>>>(line_count, cursor, nlos, dev_err);
+}
+
+void launch_flag_near(const LineTables &t, const Particles &p, const int *perm,
+                      unsigned char *flag, cudaStream_t s)
+{
+    if (p.n == 0)
+        return;
+    flag_near_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, flag);
+}
+
+long long flag_tiles(long long n) { return (n + FLAG_TILE - 1) / FLAG_TILE; }
+
+void launch_flag_count(const unsigned char *flag, long long n, unsigned *tile_count,
+                       cudaStream_t s)
+{
+    const long long nt = flag_tiles(n);
+    if (nt > 0)
+        flag_count_kernel<<<(unsigned)nt, FLAG_THREADS, 0, s>>>(flag, n, tile_count);
+}
+
+void launch_exclusive_scan(const unsigned *in, unsigned *out, unsigned *sums, int n,
+                           cudaStream_t s)
+{
+    if (n <= 0)
+        return;
+    const int nb = (n + SCAN_E - 1) / SCAN_E;
+    scan_blocks_kernel<<<nb, SCAN_T, 0, s>>>(in, out, sums, n);
+    scan_sums_kernel<<<1, SCAN_T, 0, s>>>(sums, nb);
+    add_sums_kernel<<<(n + 255) / 256, 256, 0, s>>>(out, sums, n);
+}
+
+void launch_flag_scatter(const unsigned char *flag, long long n, const unsigned *tile_start,
+                         int *out, cudaStream_t s)
+{
+    const long long nt = flag_tiles(n);
+    if (nt > 0)
+        flag_scatter_kernel<<<(unsigned)nt, FLAG_THREADS, 0, s>>>(flag, n, tile_start, out);
 }
 
 // ~64 particles per cell, at most 128^3 cells (the totals then fit one scan block)

@@ -133,6 +133,36 @@ void launch_count_pairs(const LineTables &t, const Particles &p, const int *perm
 void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
                        const long long *off, unsigned long long *cursor, int *part, double *dr2,
                        unsigned *dev_err, cudaStream_t s);
+// _near_lines: flag[i] = 1 when particle i is near any sightline (same
+// predicate as the pair search); then an ordered compaction into ascending
+// indices: tile counts (flag_tiles(n) of them), their exclusive scan
+// (n <= 2048 * 2048 tiles) and the scatter.
+void launch_flag_near(const LineTables &t, const Particles &p, const int *perm,
+                      unsigned char *flag, cudaStream_t s);
+long long flag_tiles(long long n);
+void launch_flag_count(const unsigned char *flag, long long n, unsigned *tile_count,
+                       cudaStream_t s);
+void launch_exclusive_scan(const unsigned *in, unsigned *out, unsigned *sums, int n,
+                           cudaStream_t s);
+void launch_flag_scatter(const unsigned char *flag, long long n, const unsigned *tile_start,
+                         int *out, cudaStream_t s);
+// Flux statistics (fsg_flux.cu): deterministic two-pass reductions over tau.
+// out3 = {sum exp(-scale tau), sum tau exp(-scale tau), count} over tau <= thresh;
+// part needs flux_partials(3) (resp. flux_partials(1)) doubles.
+void launch_flux_moments(const double *tau, long long n, double scale, double thresh,
+                         double *part, double *out3, cudaStream_t s);
+void launch_flux_sum(const double *tau, long long n, double scale, double *part, double *out1,
+                     cudaStream_t s);
+size_t flux_partials(int width);
+// counts[nb] += np.histogram(exp(-scale tau), edges[nb+1]) (device edges)
+void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
+                      unsigned long long *counts, cudaStream_t s);
+void launch_dflux(const double *tau, long long count, double scale, double inv_mean, double *out,
+                  cudaStream_t s);
+// power[k] += vmax sum_rows |F(k)|^2 / npix^2 over rows x nk complex (double) F
+void launch_power_accumulate(const void *F, int rows, int nk, int npix, double vmax,
+                             double *power, cudaStream_t s);
+
 // After emit: every sightline's cursor must equal its count (DEVERR_PAIR_COUNT
 // otherwise), so no slot of the pair lists is left unwritten.
 void launch_check_emit(const unsigned long long *line_count, const unsigned long long *cursor,

@@ -134,6 +134,26 @@ def tau_backward_device(ctx, nbins, kernel, box, velfac, atime, lam, gamma, fosc
     return gd, gt, gv
 
 
+def near_lines_device(ctx, box, pos, h, axis, cofm):
+    """`_near_lines` on device tensors: ascending int32 indices (device tensor) of
+    the particles within their smoothing length of any sightline."""
+    import torch
+    axis, cofm = _host_tables(axis, cofm)
+    npart = int(pos.shape[0])
+    out = torch.empty(max(npart, 1), dtype=torch.int32, device=pos.device)
+    _bind_stream(ctx)
+    n = ctypes.c_int64(0)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_near_lines_device(ctx.handle, float(box), _dptr(pos, "float32", "pos"),
+                                 _dptr(h, "float32", "h"), npart,
+                                 axis.ctypes.data_as(ctypes.c_void_p),
+                                 cofm.ctypes.data_as(ctypes.c_void_p), int(axis.shape[0]),
+                                 ctypes.c_void_p(out.data_ptr()), ctypes.byref(n), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return out[:n.value]
+
+
 def build_pairs(ctx, box, pos, h, axis, cofm):
     """Sightline-particle search on the device; returns the number of pairs."""
     axis, cofm = _host_tables(axis, cofm)

@@ -130,6 +130,60 @@ int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const
                            int64_t *npairs, char *errbuf, size_t errlen);
 
 /*
+ * Drop-in for _spectra_priv._near_lines (fake_spectra/py_module.cpp:25-99,
+ * Py_near_lines): the indices of the particles that lie within their
+ * smoothing length of at least one sightline (IndexTable::get_near_lines
+ * non-empty, fake_spectra/index_table.cpp:117-127), in ascending order, as the
+ * reference's std::set<int> returns them.  pos (npart x 3) and h are HOST
+ * pointers; out (host) must hold npart entries; *nout receives the count.
+ */
+int fsg_near_lines(double box, const float *pos, const float *h, int64_t npart,
+                   const int32_t *axis, const double *cofm, int32_t nlos, int32_t *out,
+                   int64_t *nout, char *errbuf, size_t errlen);
+
+/* The same with pos/h/out DEVICE pointers (axis/cofm HOST), on ctx's stream. */
+int fsg_near_lines_device(fsg_context *ctx, double box, const float *pos, const float *h,
+                          int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
+                          int32_t *out, int64_t *nout, char *errbuf, size_t errlen);
+
+/*
+ * Flux statistics of optical depths (float64, row-major NumLos x npix).
+ *
+ * Drop-in for _spectra_priv._rescale_mean_flux (fake_spectra/py_module.cpp:
+ * 235-282, get_mean_flux_scale / Py_mean_flux): the Newton-Raphson scale s
+ * with mean(exp(-s tau)) = mean_flux_desired over the n pixels with
+ * tau <= thresh, iterated until |s_new - s| <= tol s_new (s starts at 1 and is
+ * kept above 0).  tau is a HOST pointer here and a DEVICE pointer in the
+ * _device form; the sums run on the GPU in a fixed order.
+ */
+int fsg_rescale_mean_flux(const double *tau, int64_t n, double mean_flux_desired, double tol,
+                          double thresh, double *scale, char *errbuf, size_t errlen);
+int fsg_mean_flux_scale_device(fsg_context *ctx, const double *tau, int64_t n,
+                               double mean_flux_desired, double tol, double thresh, double *scale,
+                               char *errbuf, size_t errlen);
+
+/* mean(exp(-scale tau)) over n device values (fluxstatistics.py:96, np.mean). */
+int fsg_mean_flux_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
+                         double *mean, char *errbuf, size_t errlen);
+
+/* The counts of np.histogram(exp(-scale tau), edges) for the flux PDF
+ * (fake_spectra/fluxstatistics.py:42-51): bin j holds edges[j] <= F <
+ * edges[j+1], the last bin also F == edges[nb]; F outside [edges[0], edges[nb]]
+ * or NaN is not counted.  tau DEVICE, edges (nb+1) and counts (nb) HOST. */
+int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
+                              const double *edges, int nb, int64_t *counts, char *errbuf,
+                              size_t errlen);
+
+/* The 1-D flux power of fake_spectra/fluxstatistics.py:53-110 before its
+ * window division: power[k] = vmax / nspec * sum over sightlines of
+ * |rfft(exp(-scale tau) / mean_flux - 1)(k)|^2 / npix^2, k = 0 .. npix/2.
+ * tau DEVICE (nspec x npix), power HOST (npix/2 + 1).  The transforms are
+ * cuFFT double-precision real-to-complex, batched over sightlines. */
+int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, int64_t npix,
+                          double scale, double mean_flux, double vmax, double *power,
+                          char *errbuf, size_t errlen);
+
+/*
  * Batched form: several absorption lines of one snapshot in one call.  The
  * reference needs one _Particle_Interpolate call per line and per quantity
  * (spectra.py:801-831 compute_spectra, once per line; colden via
