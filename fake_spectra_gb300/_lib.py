@@ -38,6 +38,7 @@ EXPORTS = (
     "fsg_particle_interpolate_noalloc",
     "fsg_near_lines",
     "fsg_near_lines_device",
+    "fsg_colden_channels_device",
     "fsg_rescale_mean_flux",
     "fsg_mean_flux_scale_device",
     "fsg_mean_flux_device",
@@ -139,6 +140,9 @@ def load(path=None):
                                      ctypes.POINTER(_c_i64), _p, _c_size]
         L.fsg_near_lines_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32, _p,
                                             ctypes.POINTER(_c_i64), _p, _c_size]
+        L.fsg_colden_channels_device.argtypes = ([_p, _c_int, _c_int, _c_d, _c_d, _p, _p, _c_i64,
+                                                  _p, _p, _c_i32, _c_int, _p, _p, _p, _p,
+                                                  _c_size])
         L.fsg_rescale_mean_flux.argtypes = [_p, _c_i64, _c_d, _c_d, _c_d, ctypes.POINTER(_c_d),
                                             _p, _c_size]
         L.fsg_mean_flux_scale_device.argtypes = [_p, _p, _c_i64, _c_d, _c_d, _c_d,

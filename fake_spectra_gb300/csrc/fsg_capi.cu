@@ -963,6 +963,92 @@ int fsg_near_lines(double box, const float *pos, const float *h, int64_t npart,
     }
 }
 
+int fsg_colden_channels_device(fsg_context *ctx, int nbins, int kernel, double box,
+                               double velfac, const float *pos, const float *h, int64_t npart,
+                               const int32_t *axis, const double *cofm, int32_t nlos, int nch,
+                               const float *const *dens, double *const *out,
+                               const fsg_options *opt, char *errbuf, size_t errlen)
+{
+    try {
+        if (!ctx)
+            fail(FSG_ERR_VALUE, "ctx is NULL");
+        if (nch < 1 || nch > MAX_CHANNELS)
+            fail(FSG_ERR_VALUE, "between 1 and %d channels (got %d)", MAX_CHANNELS, nch);
+        for (int c = 0; c < nch; c++)
+            if (!dens || !out || !dens[c] || !out[c])
+                fail(FSG_ERR_VALUE, "channel %d has no density or output array", c);
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        const int precision = opt ? opt->precision : FSG_PREC_FP64;
+        if (precision != FSG_PREC_FP64 && precision != FSG_PREC_FP32)
+            fail(FSG_ERR_VALUE, "unknown precision %d", precision);
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        cudaStream_t s = ctx->stream;
+        const size_t nout = (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
+        for (int c = 0; c < nch; c++)
+            if (nout)
+                cuda_check(cudaMemsetAsync(out[c], 0, sizeof(double) * nout, s), "memset out");
+        if (nout == 0 || npart == 0) {
+            cuda_check(cudaStreamSynchronize(s), "colden channels");
+            return FSG_OK;
+        }
+        build_tables(ctx, axis, cofm, nlos, box);
+        Particles p{pos, nullptr, nullptr, nullptr, h, (long long)npart};
+        search_pairs(ctx, p, nlos);
+        if (ctx->npairs == 0)
+            return FSG_OK;
+        const LineParams lp = make_line_params(0, nbins, kernel, box, velfac, 0.0, 0.0, 0.0, 1.0,
+                                               0.0);
+        const ChannelPlan plan = colden_channels_plan(precision, nch, nbins);
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int grid = std::min(nlos, sms * plan.per_sm);
+        unsigned long long *gacc = nullptr;
+        if (!plan.smem_mode)
+            gacc = (unsigned long long *)ctx->ensure(
+                ctx->gacc, sizeof(unsigned long long) * plan.acc_words_per_cta * grid);
+        auto *bad = (int *)ctx->ensure(ctx->bad, sizeof(int) * (size_t)nch * nlos);
+        auto *nbad = (int *)ctx->ensure(ctx->nbad, sizeof(int) * MAX_CHANNELS);
+        auto *ticket = (unsigned *)ctx->ensure(ctx->ticket, sizeof(unsigned));
+        auto *err = (unsigned *)ctx->ensure(ctx->err, sizeof(unsigned));
+        cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int) * MAX_CHANNELS, s), "memset");
+        cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
+        cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
+        PairLists pl{(const long long *)ctx->off.p, (const int *)ctx->part.p,
+                     (const double *)ctx->dr2.p};
+        launch_colden_channels(lp, ctx->tables, p, pl, (const int *)ctx->line_order.p, nlos, nch,
+                               dens, out, bad, nbad, ticket, err, gacc, precision, plan, grid, s);
+        ctx->stats.gpu_launches++;
+        cuda_check(cudaGetLastError(), "colden channels launch");
+        int h_nbad[MAX_CHANNELS] = {0};
+        cuda_check(cudaMemcpyAsync(h_nbad, nbad, sizeof(int) * MAX_CHANNELS,
+                                   cudaMemcpyDeviceToHost, s), "read");
+        cuda_check(cudaStreamSynchronize(s), "colden channels");
+        int fallback = 0;
+        for (int c = 0; c < nch; c++) {
+            if (h_nbad[c] <= 0)
+                continue;
+            Particles pc = p;
+            pc.dens = dens[c];
+            launch_deposit_fallback(lp, ctx->tables, pc, pl, bad + (size_t)c * nlos, h_nbad[c],
+                                    out[c], err, s);
+            ctx->stats.gpu_launches++;
+            fallback += h_nbad[c];
+            cuda_check(cudaGetLastError(), "fallback launch");
+        }
+        ctx->stats.fallback_lines = fallback;
+        unsigned h_err = 0;
+        cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s),
+                   "read");
+        cuda_check(cudaStreamSynchronize(s), "colden channels");
+        if (h_err)
+            fail(FSG_ERR_DEVICE, "column-density kernels reported device error bits 0x%x (%s)",
+                 h_err, deverr_text(h_err).c_str());
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
 int fsg_mean_flux_scale_device(fsg_context *ctx, const double *tau, int64_t n,
                                double mean_flux_desired, double tol, double thresh, double *scale,
                                char *errbuf, size_t errlen)

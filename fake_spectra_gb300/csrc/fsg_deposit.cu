@@ -929,7 +929,7 @@ struct DepositArgs {
 
 // FMT 0: 128-bit fixed point with carries (FP64 form); 1: split (FP32 form).
 template <class R, int FMT>
-__device__ __forceinline__ void accumulate(const DepositArgs &a, R v, int j, int S,
+__device__ __forceinline__ void accumulate(unsigned *dev_err, R v, int j, int S,
                                            unsigned long long *lo, unsigned long long *hi,
                                            int *bad)
 {
@@ -942,14 +942,14 @@ __device__ __forceinline__ void accumulate(const DepositArgs &a, R v, int j, int
         if (to_fixed(v, S, l, h))
             fixed_add(lo, hi, j, l, h);
         else
-            atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+            atomicOr(dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
     } else {
         unsigned long long l;
         long long h;
         if (split_from(v, S, l, h))
             split_add(lo, hi, j, l, h);
         else
-            atomicOr(a.dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
+            atomicOr(dev_err, (unsigned)DEVERR_FIXED_OVERFLOW);
     }
 }
 
@@ -999,7 +999,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
             const unsigned m = __ballot_sync(0xffffffffu, stop);
             const int last = m ? (__ffs(m) - 1) : 31;
             if (valid && lane <= last) {
-                accumulate<R, FMT>(a, tl, bin_from(j0, koff, nbins), S, lo, hi, bad);
+                accumulate<R, FMT>(a.dev_err, tl, bin_from(j0, koff, nbins), S, lo, hi, bad);
                 if (COUNT) {
                     ct.a += c1.a;
                     ct.b += c1.b;
@@ -1025,7 +1025,7 @@ __device__ __forceinline__ void walk_colden(const DepositArgs &a, const Colden &
     static_assert(PREC == 0, "the FP32 column density walks staged pairs");
     for (int k = lane; k <= kmax; k += 32) {
         const int j = (int)(((long long)j0 + k) % nbins);
-        accumulate<double, 0>(a, c.value64(c.zlow + k), j, S, lo, hi, bad);
+        accumulate<double, 0>(a.dev_err, c.value64(c.zlow + k), j, S, lo, hi, bad);
         if (COUNT)
             ct.pixels++;
     }
@@ -1147,7 +1147,7 @@ __device__ __forceinline__ void deposit_pairs_col32(const DepositArgs &a, int ax
                     v = st.e1;
                 else
                     v = colden_interior32(st, kernel, box_f, k);
-                accumulate<float, 1>(a, v, j, S, lo, hi, bad);
+                accumulate<float, 1>(a.dev_err, v, j, S, lo, hi, bad);
                 if (COUNT)
                     ct.pixels++;
                 j += 32;
@@ -1336,6 +1336,238 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
             for (long long z = c.zlow + lane; z <= c.zhigh; z += 32)
                 atomicAdd(&row[wrap_bin(z, nbins)], c.value64(z));
         }
+    }
+}
+
+// ============================================================ column density, K channels
+// K weighted column densities of one sightline set in one pass (the weighted
+// compute_tau=0 calls of Spectra.get_velocity / get_temp /
+// get_dens_weighted_density, spectra.py:945-1043, differ only in the density
+// array).  Each pixel's kernel integral is computed once and multiplied by
+// each channel's density; per channel the bound, the fixed-point scale, the
+// rounding of every contribution and the integer sums are those of a
+// single-channel deposit, so every channel equals its single-channel result
+// bit for bit.
+struct ChannelArgs {
+    LineParams lp;
+    LineTables t;
+    Particles p;             // dens unused
+    PairLists pl;
+    const int *line_order;
+    int nlos;
+    int nch;
+    const float *dens[MAX_CHANNELS];
+    double *out[MAX_CHANNELS];
+    int *bad_lines;          // [nch][nlos]
+    int *n_bad;              // [nch]
+    unsigned *ticket;
+    unsigned *dev_err;
+    unsigned long long *gacc;   // per-CTA accumulators when not in shared memory
+    int smem_mode;
+    int chunk;
+};
+
+// Staged pair of the FP32 multi-channel form (96 bytes): the geometry of
+// StageCol32 with the three FP64 edge integrals kept density-free in double.
+struct __align__(16) StageColK {
+    int j0, kmax, flags, pad;
+    double kf0, kf1, kf2;    // kern_frac of pixels 0, kmax - 1, kmax
+    float dL0, dR0, two_zr, inv_h2, ch, pad1;
+    float dens[MAX_CHANNELS];
+};
+static_assert(sizeof(StageColK) == 96, "StageColK is six 16-byte words");
+
+__device__ __forceinline__ PairInput load_pair_ch(const ChannelArgs &a, long long e, int axis,
+                                                  int c)
+{
+    Particles p = a.p;
+    p.dens = a.dens[c];
+    return load_pair(p, a.pl, e, axis, false, a.dev_err);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(ChannelArgs a)
+{
+    extern __shared__ __align__(16) unsigned long long smem[];
+    __shared__ double red[32];
+    __shared__ int s_bad[MAX_CHANNELS];
+    __shared__ double s_B[MAX_CHANNELS];
+    __shared__ unsigned s_ticket, s_chunk;
+    const int nbins = a.lp.nbins, nch = a.nch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double btk = a.lp.vbox / nbins / a.lp.velfac;
+    const float btk_abs = (float)fabs(btk);
+    const float col_kfac = (float)(kernel_max(a.lp.kernel) * 1.001);
+    const size_t acc_words = 2 * (size_t)nbins * nch;
+    unsigned long long *acc = a.smem_mode ? smem : a.gacc + (size_t)blockIdx.x * acc_words;
+    StageColK *sw = reinterpret_cast<StageColK *>(smem + (a.smem_mode ? acc_words : 0)) +
+                    warp * a.chunk;
+    if (threadIdx.x == 0)
+        s_ticket = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    unsigned ticket = s_ticket;
+    while (ticket < (unsigned)a.nlos) {
+        const int line = a.line_order[ticket];
+        const int axis = a.t.axis[line];
+        const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
+        // 1. per-channel bounds, summed exactly as the single-channel deposit sums them
+        for (int c = 0; c < nch; c++) {
+            double b = 0.0;
+            for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+                const PairInput in = load_pair_ch(a, e, axis, c);
+                b += PREC == 1 ? colden_pair_bound32(a.lp, in, btk_abs, col_kfac)
+                               : colden_pair_bound(a.lp, in, btk);
+            }
+            const double B = block_sum(b, red);
+            if (threadIdx.x == 0) {
+                s_B[c] = B;
+                s_bad[c] = !isfinite(B);
+            }
+        }
+        for (size_t j = threadIdx.x; j < acc_words; j += blockDim.x)
+            acc[j] = 0ull;
+        if (threadIdx.x == 0)
+            s_chunk = 0u;
+        __syncthreads();
+        int S[MAX_CHANNELS];
+        bool live[MAX_CHANNELS];
+#pragma unroll
+        for (int c = 0; c < MAX_CHANNELS; c++) {
+            live[c] = c < nch && !s_bad[c] && s_B[c] > 0.0;
+            S[c] = live[c] ? (PREC == 0 ? 124 : SPLIT_TOP) - ilogb(s_B[c]) : 0;
+        }
+        // 2. deposit: chunks of pairs, one lane per pair of the chunk sets it up
+        for (;;) {
+            unsigned q = 0;
+            if (lane == 0)
+                q = atomicAdd(&s_chunk, 1u);
+            q = __shfl_sync(0xffffffffu, q, 0);
+            const long long cb = e0 + (long long)q * a.chunk;
+            if (cb >= e1)
+                break;
+            const int n = (int)min((long long)a.chunk, e1 - cb);
+            if (lane < n) {
+                const PairInput in = load_pair_ch(a, cb + lane, axis, 0);
+                StageColK st;
+                Colden col;
+                st.flags = 0;
+                if (!col.setup(a.lp, in, btk)) {
+                    st.flags = COL_SKIP;
+                } else if (!col.ok) {
+                    st.flags = COL_BAD;
+                } else {
+                    st.j0 = wrap_bin(col.zlow, nbins);
+                    st.kmax = (int)col.kmax;
+                    const auto kf = [&](long long z) {
+                        const double plow = btk * (double)z - col.pos1;
+                        return kern_frac<double>(a.lp.kernel, plow, plow + btk, col.smooth,
+                                                 col.dr2, col.zrange);
+                    };
+                    if constexpr (PREC == 1) {
+                        st.kf0 = kf(col.zlow);
+                        st.kf1 = col.kmax >= 2 ? kf(col.zlow + col.kmax - 1) : 0.0;
+                        st.kf2 = col.kmax >= 1 ? kf(col.zhigh) : 0.0;
+                        st.dL0 = col.dL0;
+                        st.dR0 = col.dR0;
+                        st.two_zr = col.two_zr;
+                        st.inv_h2 = col.inv_h2;
+                        st.ch = col.ch;
+                    }
+                }
+                const int ip = a.pl.part[cb + lane];
+#pragma unroll
+                for (int c = 0; c < MAX_CHANNELS; c++)
+                    st.dens[c] = (c < nch && (unsigned long long)(long long)ip <
+                                                 (unsigned long long)a.p.n)
+                                     ? __ldg(&a.dens[c][ip]) : 0.f;
+                sw[lane] = st;
+            }
+            __syncwarp();
+            for (int k2 = 0; k2 < n; k2++) {
+                const StageColK st = sw[k2];
+                if (st.flags == COL_SKIP)
+                    continue;
+                if (st.flags == COL_BAD) {
+                    if (lane == 0)
+                        atomicOr(a.dev_err, (unsigned)DEVERR_WINDOW_LIMIT);
+                    for (int c = 0; c < nch; c++)
+                        s_bad[c] = 1;
+                    continue;
+                }
+                // the FP64 form needs the pair's geometry again: rebuild it from the pair
+                Colden col;
+                if constexpr (PREC == 0) {
+                    const PairInput in = load_pair_ch(a, cb + k2, axis, 0);
+                    col.setup(a.lp, in, btk);
+                }
+                int j = st.j0 + lane;
+                while (j >= nbins)
+                    j -= nbins;
+                for (int k = lane; k <= st.kmax; k += 32) {
+                    if constexpr (PREC == 0) {
+                        const double plow = btk * (double)(col.zlow + k) - col.pos1;
+                        const double f = kern_frac<double>(a.lp.kernel, plow, plow + btk,
+                                                           col.smooth, col.dr2, col.zrange);
+#pragma unroll
+                        for (int c = 0; c < MAX_CHANNELS; c++)
+                            if (live[c])
+                                accumulate<double, 0>(a.dev_err, (double)st.dens[c] * f, j, S[c],
+                                                      acc + 2 * (size_t)c * nbins,
+                                                      acc + (2 * (size_t)c + 1) * nbins,
+                                                      &s_bad[c]);
+                    } else {
+                        const bool edge = k == 0 || k >= st.kmax - 1;
+                        const double fe = k == 0 ? st.kf0 : (k == st.kmax ? st.kf2 : st.kf1);
+                        float f32 = 0.f;
+                        if (!edge) {
+                            StageCol32 g;
+                            g.kmax = st.kmax;
+                            g.dens_f = 1.f;
+                            g.dL0 = st.dL0;
+                            g.dR0 = st.dR0;
+                            g.two_zr = st.two_zr;
+                            g.inv_h2 = st.inv_h2;
+                            g.ch = st.ch;
+                            // unit density: the single-channel form multiplies this by dens
+                            f32 = colden_interior32(g, a.lp.kernel, (float)btk, k);
+                        }
+#pragma unroll
+                        for (int c = 0; c < MAX_CHANNELS; c++)
+                            if (live[c]) {
+                                const float v = edge ? (float)((double)st.dens[c] * fe)
+                                                     : st.dens[c] * f32;
+                                accumulate<float, 1>(a.dev_err, v, j, S[c],
+                                                     acc + 2 * (size_t)c * nbins,
+                                                     acc + (2 * (size_t)c + 1) * nbins,
+                                                     &s_bad[c]);
+                            }
+                    }
+                    j += 32;
+                    while (j >= nbins)
+                        j -= nbins;
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        // 3. flush each channel's row (or hand the line to the fallback)
+        for (int c = 0; c < nch; c++) {
+            if (s_bad[c]) {
+                if (threadIdx.x == 0)
+                    a.bad_lines[(size_t)c * a.nlos + atomicAdd(&a.n_bad[c], 1)] = line;
+            } else if (s_B[c] > 0.0) {
+                double *row = a.out[c] + (size_t)line * nbins;
+                const unsigned long long *lo = acc + 2 * (size_t)c * nbins, *hi = lo + nbins;
+                for (int j = threadIdx.x; j < nbins; j += blockDim.x)
+                    row[j] = PREC == 0 ? from_fixed(lo[j], hi[j], S[c])
+                                       : from_split(lo[j], hi[j], S[c]);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_ticket = atomicAdd(a.ticket, 1u);
+        __syncthreads();
+        ticket = s_ticket;
     }
 }
 
@@ -1796,6 +2028,83 @@ int tau_backward_resident_ctas()
                          (int)GRAD_SMEM);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, grad_kernel, GRAD_THREADS, GRAD_SMEM);
     return n;
+}
+
+
+// ---------------------------------------------------------------- K channels
+namespace {
+constexpr int CHAN_CHUNK = 32;
+int chan_threads(int precision) { return precision == 0 ? 256 : 512; }
+size_t chan_smem(int precision, int nch, int nbins, int smem_mode)
+{
+    return (smem_mode ? 2 * sizeof(unsigned long long) * nbins * nch : 0) +
+           (size_t)(chan_threads(precision) / 32) * CHAN_CHUNK * sizeof(StageColK);
+}
+template <int PREC>
+void chan_attr(size_t smem)
+{
+    cudaFuncSetAttribute(colden_channels_kernel<PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+}
+}  // namespace
+
+ChannelPlan colden_channels_plan(int precision, int nch, int nbins)
+{
+    ChannelPlan pl{};
+    pl.threads = chan_threads(precision);
+    const size_t cap = (size_t)(max_smem_optin() - STATIC_SMEM_RESERVE);
+    pl.smem_mode = chan_smem(precision, nch, nbins, 1) <= cap;
+    pl.smem = chan_smem(precision, nch, nbins, pl.smem_mode);
+    int n = 0;
+    if (precision == 0) {
+        chan_attr<0>(pl.smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, colden_channels_kernel<0>, pl.threads,
+                                                      pl.smem);
+    } else {
+        chan_attr<1>(pl.smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, colden_channels_kernel<1>, pl.threads,
+                                                      pl.smem);
+    }
+    pl.per_sm = n > 0 ? n : 1;
+    pl.acc_words_per_cta = 2 * (size_t)nbins * nch;
+    return pl;
+}
+
+void launch_colden_channels(const LineParams &lp, const LineTables &t, const Particles &p,
+                            const PairLists &pl, const int *line_order, int nlos, int nch,
+                            const float *const *dens, double *const *out, int *bad_lines,
+                            int *n_bad, unsigned *ticket, unsigned *dev_err,
+                            unsigned long long *gacc, int precision, const ChannelPlan &plan,
+                            int grid, cudaStream_t s)
+{
+    if (nlos == 0 || nch == 0)
+        return;
+    ChannelArgs a;
+    a.lp = lp;
+    a.t = t;
+    a.p = p;
+    a.pl = pl;
+    a.line_order = line_order;
+    a.nlos = nlos;
+    a.nch = nch;
+    for (int c = 0; c < MAX_CHANNELS; c++) {
+        a.dens[c] = c < nch ? dens[c] : nullptr;
+        a.out[c] = c < nch ? out[c] : nullptr;
+    }
+    a.bad_lines = bad_lines;
+    a.n_bad = n_bad;
+    a.ticket = ticket;
+    a.dev_err = dev_err;
+    a.gacc = gacc;
+    a.smem_mode = plan.smem_mode;
+    a.chunk = CHAN_CHUNK;
+    if (precision == 0) {
+        chan_attr<0>(plan.smem);
+        colden_channels_kernel<0><<<grid, plan.threads, plan.smem, s>>>(a);
+    } else {
+        chan_attr<1>(plan.smem);
+        colden_channels_kernel<1><<<grid, plan.threads, plan.smem, s>>>(a);
+    }
 }
 
 }  // namespace fsg

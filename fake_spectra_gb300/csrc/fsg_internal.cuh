@@ -146,6 +146,24 @@ void launch_exclusive_scan(const unsigned *in, unsigned *out, unsigned *sums, in
                            cudaStream_t s);
 void launch_flag_scatter(const unsigned char *flag, long long n, const unsigned *tile_start,
                          int *out, cudaStream_t s);
+// K weighted column densities in one pass (colden_channels_kernel): per
+// channel a density array in and a (nlos x nbins) row block out; bad_lines
+// [nch][nlos] and n_bad[nch] list the lines each channel leaves to the
+// fallback.  Outside shared memory the accumulators take grid x
+// acc_words_per_cta words of gacc.
+constexpr int MAX_CHANNELS = 8;
+struct ChannelPlan {
+    int threads, smem_mode, per_sm;
+    size_t smem, acc_words_per_cta;
+};
+ChannelPlan colden_channels_plan(int precision, int nch, int nbins);
+void launch_colden_channels(const LineParams &lp, const LineTables &t, const Particles &p,
+                            const PairLists &pl, const int *line_order, int nlos, int nch,
+                            const float *const *dens, double *const *out, int *bad_lines,
+                            int *n_bad, unsigned *ticket, unsigned *dev_err,
+                            unsigned long long *gacc, int precision, const ChannelPlan &plan,
+                            int grid, cudaStream_t s);
+
 // Flux statistics (fsg_flux.cu): deterministic two-pass reductions over tau.
 // out3 = {sum exp(-scale tau), sum tau exp(-scale tau), count} over tau <= thresh;
 // part needs flux_partials(3) (resp. flux_partials(1)) doubles.

@@ -154,6 +154,35 @@ def near_lines_device(ctx, box, pos, h, axis, cofm):
     return out[:n.value]
 
 
+def colden_channels_device(ctx, nbins, kernel, box, velfac, pos, h, axis, cofm, dens,
+                           precision="fp64"):
+    """Several weighted column densities in one pass: one (nlos, nbins) float64
+    device tensor per float32 density tensor in `dens` (at most 8), each equal to
+    the compute_tau=0 interpolation with that density."""
+    import torch
+    axis, cofm = _host_tables(axis, cofm)
+    nlos = int(axis.shape[0])
+    dens = list(dens)
+    outs = [torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device)
+            for _ in dens]
+    dp = (ctypes.c_void_p * max(len(dens), 1))(*[_dptr(d, "float32", "dens").value
+                                                 for d in dens])
+    op = (ctypes.c_void_p * max(len(outs), 1))(*[o.data_ptr() for o in outs])
+    _bind_stream(ctx)
+    opt = _lib.make_options(precision)
+    eb = _lib.errbuf()
+    L = _lib.load()
+    rc = L.fsg_colden_channels_device(ctx.handle, int(nbins), int(kernel), float(box),
+                                      float(velfac), _dptr(pos, "float32", "pos"),
+                                      _dptr(h, "float32", "h"), int(pos.shape[0]),
+                                      axis.ctypes.data_as(ctypes.c_void_p),
+                                      cofm.ctypes.data_as(ctypes.c_void_p), nlos, len(dens),
+                                      ctypes.cast(dp, ctypes.c_void_p),
+                                      ctypes.cast(op, ctypes.c_void_p), ctypes.byref(opt), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    return outs
+
+
 def build_pairs(ctx, box, pos, h, axis, cofm):
     """Sightline-particle search on the device; returns the number of pairs."""
     axis, cofm = _host_tables(axis, cofm)

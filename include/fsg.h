@@ -147,6 +147,22 @@ int fsg_near_lines_device(fsg_context *ctx, double box, const float *pos, const 
                           int32_t *out, int64_t *nout, char *errbuf, size_t errlen);
 
 /*
+ * Several weighted column densities in one pass: channel c is the
+ * compute_tau=0 interpolation with density array dens[c] (DEVICE), written to
+ * out[c] (DEVICE, nlos x nbins).  This replaces the weighted column-density
+ * calls of Spectra.get_velocity, get_temp and get_dens_weighted_density
+ * (fake_spectra/spectra.py:945-1043: one _Particle_Interpolate(0, ...) per
+ * weight); every channel equals its single-channel result bit for bit.
+ * 1 <= nch <= 8; pos/h DEVICE, axis/cofm HOST; opt->precision as for the
+ * interpolation.
+ */
+int fsg_colden_channels_device(fsg_context *ctx, int nbins, int kernel, double box,
+                               double velfac, const float *pos, const float *h, int64_t npart,
+                               const int32_t *axis, const double *cofm, int32_t nlos, int nch,
+                               const float *const *dens, double *const *out,
+                               const fsg_options *opt, char *errbuf, size_t errlen);
+
+/*
  * Flux statistics of optical depths (float64, row-major NumLos x npix).
  *
  * Drop-in for _spectra_priv._rescale_mean_flux (fake_spectra/py_module.cpp:

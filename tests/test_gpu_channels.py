@@ -1,0 +1,64 @@
+"""Weighted column densities in one pass (fsg_colden_channels_device): every
+channel equals the single-channel compute_tau=0 interpolation bit for bit, in
+both forms, with the accumulators in shared memory and in global memory, and
+with a channel whose sightlines go to the non-finite fallback."""
+import numpy as np
+import pytest
+
+from fake_spectra_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _weights(w):
+    # the weights of Spectra.get_velocity / get_temp / get_dens_weighted_density
+    rng = np.random.default_rng(11)
+    d = w.dens["HI"]
+    return [d, d * w.vel[:, 0], d * w.vel[:, 1], d * w.vel[:, 2], d * w.temp,
+            d * rng.lognormal(0, 1, size=d.shape).astype(np.float32)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("nbins", [111, 3000])
+def test_channels_equal_single_calls(ctx, precision, nbins):
+    import torch
+    from fake_spectra_gb300 import interp as I
+    w = synth.config0()
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+    pos, vel, temp, hh = T(w.pos), T(w.vel), T(w.temp), T(w.hh)
+    dens = [T(x) for x in _weights(w)]
+    if nbins == 3000:
+        dens = dens + dens[:2]    # 8 channels: accumulators do not fit in shared memory
+    outs = I.colden_channels_device(ctx, nbins, w.kernel, w.box, w.velfac, pos, hh, w.axis,
+                                    w.cofm, dens, precision=precision)
+    assert len(outs) == len(dens)
+    for c, d in enumerate(dens):
+        args = list(w.call_args(synth.LYA, 0))
+        args[1] = nbins
+        ref = I.particle_interpolate_device(ctx, *args[:11], pos, vel, d, temp, hh, w.axis,
+                                            w.cofm, precision=precision)
+        assert torch.equal(outs[c], ref), c
+
+
+def test_channels_nonfinite_fallback(ctx, port):
+    import torch
+    from fake_spectra_gb300 import interp as I
+    w = synth.config0()
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+    pos, vel, temp, hh = T(w.pos), T(w.vel), T(w.temp), T(w.hh)
+    d0 = w.dens["HI"].copy()
+    d1 = d0.copy()
+    off, part, _ = port.near_particles(w.pos, w.hh, w.axis, w.cofm, w.box)
+    d1[part[off[3]]] = np.inf    # one particle of sightline 3
+    outs = I.colden_channels_device(ctx, w.nbins, w.kernel, w.box, w.velfac, pos, hh, w.axis,
+                                    w.cofm, [T(d0), T(d1)], precision="fp32")
+    for c, d in enumerate((d0, d1)):
+        args = w.call_args(synth.LYA, 0)
+        ref = I.particle_interpolate_device(ctx, *args[:11], pos, vel, T(d), temp, hh, w.axis,
+                                            w.cofm, precision="fp32")
+        a, b = outs[c].cpu().numpy(), ref.cpu().numpy()
+        assert np.array_equal(np.isinf(a), np.isinf(b))
+        fin = np.isfinite(b)
+        np.testing.assert_allclose(a[fin], b[fin], rtol=1e-12, atol=0)
+    assert np.isinf(outs[1][3].cpu().numpy()).any()
+    assert torch.isfinite(outs[0]).all()
