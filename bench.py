@@ -53,6 +53,14 @@ FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f).get("hbm_gbs"))
+    except Exception:
+        return None
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -71,6 +79,8 @@ def parse_args():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-bwd", action="store_true")
+    p.add_argument("--no-extra", action="store_true",
+                   help="skip the multi-channel column density and flux statistics sections")
     return p.parse_args()
 
 
@@ -305,6 +315,10 @@ def main():
                               "evals": evals, "flops_per_eval": F_EVAL,
                               "evals_core": cnt["evals_core"], "evals_wing": cnt["evals_wing"],
                               "evals_wing_multipole": mp,
+                              "samples_by_path": {"multipole": mp // 7,
+                                                  "wing": cnt["samples_wing_path"],
+                                                  "core": cnt["samples_core_path"],
+                                                  "mixed": cnt["samples_mixed_path"]},
                               "evals_other": cnt["evals_other"], "pixels": cnt["pixels"],
                               "launches_timed": 1,
                               "deposit_ms_per_launch": dep_mean},
@@ -384,6 +398,63 @@ def main():
                           "tau_pixels_per_s": ntau * pixels / (msb * 1e-3),
                           "graph": "one CUDA graph of all deposits after one sightline search"}
         del outs
+
+    # ---- weighted column densities: 5 channels fused against 5 single calls (FP32)
+    if not args.no_extra:
+        d = w.dens["HI"]
+        chans = [d, d * w.vel[:, 0], d * w.vel[:, 1], d * w.vel[:, 2], d * w.temp]
+        cargs = list(w.call_args(lya, 0))
+
+        def fused():
+            return interp.colden_channels_device(ctx, w.nbins, w.kernel, w.box, w.velfac, w.pos,
+                                                 w.hh, w.axis, w.cofm, chans, precision="fp32")
+
+        def singles():
+            r = []
+            for dc in chans:
+                cargs[13] = dc
+                r.append(interp.particle_interpolate_device(ctx, *cargs, precision="fp32"))
+            return r
+        timings = {}
+        for name, fn in (("fused", fused), ("single_calls", singles)):
+            outs = fn()
+            del outs
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            outs = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            timings[name] = e0.elapsed_time(e1)
+            del outs
+        del chans
+        res["colden_channels"] = {"channels": 5, "ms_fused": timings["fused"],
+                                  "ms_single_calls": timings["single_calls"],
+                                  "weights": "dens x {1, v_x, v_y, v_z, T}",
+                                  "form": "FP32, one search + one kernel vs 5 calls"}
+
+        # ---- flux statistics of the FP32 tau still in HBM (HBM-bound reductions)
+        from fake_spectra_gb300 import fluxstatistics as fstat
+        hbm = measured_hbm_gbs()
+        ntau = tau32.numel()
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            torch.cuda.synchronize()
+            return r, (time.perf_counter() - t0) * 1e3
+        fstat._context()
+        scale, ms_mf = timed(lambda: fstat.mean_flux(tau32, 0.7))
+        _, ms_pdf = timed(lambda: fstat.flux_pdf(tau32, 20, None))
+        _, ms_pow = timed(lambda: fstat.flux_power(tau32, w.nbins * 1.0, 8, None, False))
+        res["flux_statistics"] = {
+            "tau_pixels": ntau, "mean_flux_ms": ms_mf, "scale": scale,
+            "flux_pdf_ms": ms_pdf, "flux_power_ms": ms_pow,
+            "pdf_hbm_frac": (ntau * 8 / (ms_pdf * 1e-3) / 1e9) / hbm if hbm else None,
+            "note": "wall time of each call (host API, tau resident in HBM); the PDF pass reads "
+                    "8 B per pixel once, against the measured HBM copy bandwidth"}
 
     # ---- differentiation form: forward and forward+backward on the 128^3 workload
     if not args.no_bwd:

@@ -63,7 +63,9 @@ class Stats(ctypes.Structure):
     _fields_ = [("npairs", _c_i64), ("gpu_launches", _c_i64), ("fallback_lines", _c_i32),
                 ("reserved", _c_i32), ("ms_search", _c_d), ("ms_deposit", _c_d),
                 ("evals_core", _c_i64), ("evals_wing", _c_i64), ("evals_other", _c_i64),
-                ("pixels", _c_i64), ("evals_wing_multipole", _c_i64)]
+                ("pixels", _c_i64), ("evals_wing_multipole", _c_i64),
+                ("samples_wing_path", _c_i64), ("samples_core_path", _c_i64),
+                ("samples_mixed_path", _c_i64)]
 
 
 class Line(ctypes.Structure):
@@ -202,7 +204,10 @@ class Context:
                 "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
                 "ms_deposit": float(s.ms_deposit), "evals_core": int(s.evals_core),
                 "evals_wing": int(s.evals_wing), "evals_other": int(s.evals_other),
-                "pixels": int(s.pixels), "evals_wing_multipole": int(s.evals_wing_multipole)}
+                "pixels": int(s.pixels), "evals_wing_multipole": int(s.evals_wing_multipole),
+                "samples_wing_path": int(s.samples_wing_path),
+                "samples_core_path": int(s.samples_core_path),
+                "samples_mixed_path": int(s.samples_mixed_path)}
 
     def close(self):
         if self._h:

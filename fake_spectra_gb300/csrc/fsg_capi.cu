@@ -408,8 +408,8 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     const bool count = opt && opt->count_work;
     unsigned long long *ctr = nullptr;
     if (count) {
-        ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 5);
-        cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 5, s), "memset");
+        ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 8);
+        cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 8, s), "memset");
     }
     auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
     auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
@@ -440,13 +440,16 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
     c->stats.ms_deposit = ms;
     if (count) {
-        unsigned long long h_ctr[5];
+        unsigned long long h_ctr[8];
         cuda_check(cudaMemcpy(h_ctr, ctr, sizeof h_ctr, cudaMemcpyDeviceToHost), "read counters");
         c->stats.evals_core = (int64_t)h_ctr[0];
         c->stats.evals_wing = (int64_t)h_ctr[1];
         c->stats.evals_other = (int64_t)h_ctr[2];
         c->stats.pixels = (int64_t)h_ctr[3];
         c->stats.evals_wing_multipole = (int64_t)h_ctr[4];
+        c->stats.samples_wing_path = (int64_t)h_ctr[5];
+        c->stats.samples_core_path = (int64_t)h_ctr[6];
+        c->stats.samples_mixed_path = (int64_t)h_ctr[7];
     }
     if (h_err)
         fail(FSG_ERR_DEVICE, "deposit kernel reported device error bits 0x%x (%s)", h_err,

@@ -335,8 +335,10 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
 // Work counters of the counting variant (per lane, reduced per CTA at exit):
 // a core-branch evals, b wing-branch evals, c other evals, pixels, and d the
 // wing evals among b that were summed through the multipole form.
+// e, f, g: node-sum samples through the all-wing, all-core and mixed paths
+// (the multipole path is d / 7).
 struct Counters {
-    unsigned long long a, b, c, pixels, d;
+    unsigned long long a = 0, b = 0, c = 0, pixels = 0, d = 0, e = 0, f = 0, g = 0;
 };
 
 __device__ __forceinline__ double nan_d() { return __longlong_as_double(0x7ff8000000000000ll); }
@@ -641,16 +643,20 @@ struct Tau32 {
 #pragma unroll
             for (int i = 0; i < NODES; ++i)
                 total = fmaf(voigt_wing32(u[i], vc), w[i], total);
-            if (COUNT)
+            if (COUNT) {
                 ct.b += NODES;
+                ct.e++;
+            }
             return total;
         }
         if (__all_sync(0xffffffffu, core)) {
 #pragma unroll
             for (int i = 0; i < NODES; ++i)
                 total = fmaf(voigt_core32(u[i], vc, tab), w[i], total);
-            if (COUNT)
+            if (COUNT) {
                 ct.a += NODES;
+                ct.f++;
+            }
             return total;
         }
         unsigned nn = 0;
@@ -660,6 +666,7 @@ struct Tau32 {
         if (COUNT) {
             ct.a += nn;
             ct.b += NODES - nn;
+            ct.g++;
         }
         return total;
     }
@@ -921,7 +928,7 @@ struct DepositArgs {
     int *n_bad;
     unsigned *dev_err;
     unsigned long long *gacc;   // global accumulators when not in shared memory
-    unsigned long long *counters;   // [5] (counting variant only)
+    unsigned long long *counters;   // [8] (counting variant only)
     int smem_mode;
     int persistent;
     int chunk;                      // pairs staged per warp (FP32 tau form)
@@ -986,7 +993,7 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
             const int k = step + lane;
             const bool valid = k < half;
             const int koff = dir == 0 ? k : -1 - k;
-            Counters c1 = {0, 0, 0, 0, 0};
+            Counters c1{};
             R tl = (R)0;
             if constexpr (PREC == 0) {
                 if (valid)
@@ -1005,6 +1012,9 @@ __device__ __forceinline__ void walk_tau(const DepositArgs &a, const P &s, int S
                     ct.b += c1.b;
                     ct.c += c1.c;
                     ct.d += c1.d;
+                    ct.e += c1.e;
+                    ct.f += c1.f;
+                    ct.g += c1.g;
                     ct.pixels++;
                 }
             }
@@ -1041,7 +1051,7 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
     Tau64 s;
     if (!s.setup(a.lp, in))
         return;
-    Counters c = {0, 0, 0, 0, 0};
+    Counters c{};
     walk_tau<0, COUNT, 1>(a, s, S, lo, hi, bad, lane, nullptr, c);
     if (COUNT) {
         ct.c += c.a + c.b + c.c;
@@ -1172,7 +1182,7 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const double boxtokpc = a.lp.vbox / nbins / a.lp.velfac;
     const double bintov_d = a.lp.vbox / nbins;
-    Counters ct = {0, 0, 0, 0, 0};
+    Counters ct{};
     if constexpr (PREC == 1 && TAU)
         stage_voigt32(vtab);
     const Bound32 bk(a.lp);
@@ -1278,6 +1288,9 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         atomicAdd(&a.counters[2], ct.c);
         atomicAdd(&a.counters[3], ct.pixels);
         atomicAdd(&a.counters[4], ct.d);
+        atomicAdd(&a.counters[5], ct.e);
+        atomicAdd(&a.counters[6], ct.f);
+        atomicAdd(&a.counters[7], ct.g);
     }
 }
 
@@ -1299,7 +1312,7 @@ __global__ void __launch_bounds__(256) fallback_kernel(LineParams lp, LineTables
     const double boxtokpc = lp.vbox / nbins / lp.velfac;
     double *row = out + (size_t)line * nbins;
     const long long e0 = pl.off[line], e1 = pl.off[line + 1];
-    Counters ct = {0, 0, 0, 0, 0};
+    Counters ct{};
     for (long long e = e0 + warp; e < e1; e += nwarps) {
         const PairInput in = load_pair(p, pl, e, axis, TAU, dev_err);
         if (TAU) {
@@ -1635,7 +1648,7 @@ __device__ __noinline__ void grad_pair_careful(const GradArgs &a, const PairInpu
     const double amp_v = s.ampd / a.lp.velfac;   // amp dens / velfac
     const double amp_nod = (s.ampd / ((double)in.dens != 0.0 ? (double)in.dens : 1.0)) /
                            a.lp.velfac;
-    Counters ct = {0, 0, 0, 0, 0};
+    Counters ct{};
     for (int dir = 0; dir < 2; dir++) {
         for (int step = 0; step < half; step += 32) {
             const int k = step + lane;

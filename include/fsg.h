@@ -65,6 +65,11 @@ typedef struct {
     int64_t pixels;          /* pixel contributions                             */
     int64_t evals_wing_multipole; /* wing evaluations summed by the far-wing
                                      multipole form (FP32; subset of evals_wing) */
+    /* FP32 node-sum samples (7 evaluations each) by warp-uniform path; the
+     * multipole path has evals_wing_multipole / 7 */
+    int64_t samples_wing_path;   /* every node asymptotic                  */
+    int64_t samples_core_path;   /* every node in the tabulated core       */
+    int64_t samples_mixed_path;  /* node by node                           */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
