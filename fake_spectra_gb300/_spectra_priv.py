@@ -16,7 +16,9 @@ runs on the GPU through libfsg's C ABI; there is no CPU path.
 Differences from the reference, all for inputs on which the reference has
 undefined behaviour: axis values outside {1, 2, 3}, non-finite sightline
 positions, pos/vel arrays that are not (Npart, 3), and a non-positive box size
-raise ValueError; the Voronoi kernel (kernel=2) raises NotImplementedError.
+raise ValueError.  The Voronoi-mesh kernel (kernel=2) runs in the FP64 form
+whatever precision is asked for, and a cell whose points along a sightline are
+not contiguous (where the reference calls exit) raises ValueError.
 """
 import ctypes
 
@@ -105,8 +107,6 @@ def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1):
         temp = np.ascontiguousarray(temp)
     out = np.zeros((nlos, nbins), dtype=np.float64)
     if nlos == 0 or nbins == 0:
-        if kernel == 2:
-            raise NotImplementedError("the Voronoi-mesh kernel (kernel == 2) is not implemented")
         return out
     L = _lib.load()
     opt = _lib.make_options(precision, threads, persistent)

@@ -19,7 +19,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libfsg.so")
 
 SOURCES = ["fsg_capi.cu", "fsg_index.cu", "fsg_deposit.cu", "fsg_peak.cu", "fsg_noalloc.cu",
-           "fsg_flux.cu"]
+           "fsg_flux.cu", "fsg_voronoi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -80,6 +80,7 @@ struct fsg_context {
     DevBuf skey, sperm, shist, sstart, ssums;                // particle ordering
     DevBuf flag, tcount, tstart, tsums, idx;                 // _near_lines
     DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
+    DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // host mirrors
     std::vector<long long> h_off;
@@ -116,7 +117,7 @@ struct fsg_context {
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
-                          &ffft, &fpower};
+                          &ffft, &fpower, &vseg, &vscratch, &vcofm};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -129,7 +130,7 @@ struct fsg_context {
 namespace {
 
 void validate_common(int nbins, int kernel, double box, int64_t npart, int32_t nlos,
-                     const int32_t *axis, const double *cofm)
+                     const int32_t *axis, const double *cofm, bool allow_voronoi = false)
 {
     if (nbins < 0)
         fail(FSG_ERR_VALUE, "nbins must be non-negative (got %d)", nbins);
@@ -138,8 +139,9 @@ void validate_common(int nbins, int kernel, double box, int64_t npart, int32_t n
     if (npart > 2147483647LL)
         fail(FSG_ERR_VALUE, "at most 2^31-1 particles (particle indices are int, as in the "
                             "reference's std::map<int, double>)");
-    if (kernel == VORONOI)
-        fail(FSG_ERR_NOT_IMPLEMENTED, "the Voronoi-mesh kernel (kernel == 2) is not implemented");
+    if (kernel == VORONOI && !allow_voronoi)
+        fail(FSG_ERR_NOT_IMPLEMENTED, "the Voronoi-mesh kernel (kernel == 2) is supported by "
+                                      "the single-line interpolation entry points only");
     if (!(box > 0.0) || !std::isfinite(box))
         fail(FSG_ERR_VALUE, "box size must be positive and finite (got %g)", box);
     for (int i = 0; i < nlos; i++) {
@@ -384,7 +386,7 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
 
 // 3. deposit into out (device, nlos*nbins)
 void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
-             const fsg_options *opt)
+             const fsg_options *opt, const float2 *seg = nullptr)
 {
     cudaStream_t s = c->stream;
     const int nlos = c->nlos;
@@ -399,7 +401,8 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
         c->stats.ms_deposit = 0;
         return;
     }
-    PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
+    PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p,
+                 seg};
     const DepositLaunch cfg = deposit_config(c, lp, opt);
     unsigned long long *gacc = nullptr;
     if (!cfg.smem_mode) {
@@ -485,13 +488,17 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
     cfg.precision = opt ? opt->precision : FSG_PREC_FP64;
     if (cfg.precision != FSG_PREC_FP64 && cfg.precision != FSG_PREC_FP32)
         fail(FSG_ERR_VALUE, "unknown precision %d", cfg.precision);
+    // the Voronoi mesh (kernel 2) has no FP32 form: it deposits in FP64
+    const bool vor = lp.kernel == VORONOI;
+    if (vor)
+        cfg.precision = FSG_PREC_FP64;
     const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
-    cfg.threads = (opt && opt->threads > 0) ? opt->threads : tmax;
+    cfg.threads = (opt && opt->threads > 0 && !vor) ? opt->threads : tmax;
     if (cfg.threads % 32 || cfg.threads > tmax)
         fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
     deposit_plan(cfg, lp.compute_tau, lp.nbins);
-    cfg.persistent = (opt && opt->persistent >= 0) ? opt->persistent
-                                                    : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
+    cfg.persistent = (opt && opt->persistent >= 0 && !vor)
+                         ? opt->persistent : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     const int per_sm = std::max(1, deposit_resident_ctas(cfg, lp.compute_tau, lp.nbins));
@@ -633,6 +640,76 @@ fsg_context *default_context()
     return g_default[dev];
 }
 
+// Pairs of every sightline in ascending particle order (the reference's
+// std::map order, which the Voronoi cell assignment depends on).
+void sort_pairs_by_particle(fsg_context *c)
+{
+    const long long total = c->npairs;
+    if (total <= 0)
+        return;
+    cudaStream_t s = c->stream;
+    std::vector<int> part((size_t)total);
+    std::vector<double> dr2((size_t)total);
+    cuda_check(cudaMemcpyAsync(part.data(), c->part.p, sizeof(int) * total, cudaMemcpyDeviceToHost,
+                               s), "D2H pairs");
+    cuda_check(cudaMemcpyAsync(dr2.data(), c->dr2.p, sizeof(double) * total,
+                               cudaMemcpyDeviceToHost, s), "D2H pairs");
+    cuda_check(cudaStreamSynchronize(s), "D2H pairs");
+    std::vector<std::pair<int, double>> tmp;
+    for (int l = 0; l < c->nlos; l++) {
+        const long long a = c->h_off[l], b = c->h_off[l + 1];
+        tmp.resize((size_t)(b - a));
+        for (long long e = a; e < b; e++)
+            tmp[e - a] = {part[e], dr2[e]};
+        std::sort(tmp.begin(), tmp.end(),
+                  [](const std::pair<int, double> &x, const std::pair<int, double> &y) {
+                      return x.first < y.first;
+                  });
+        for (long long e = a; e < b; e++) {
+            part[e] = tmp[e - a].first;
+            dr2[e] = tmp[e - a].second;
+        }
+    }
+    cuda_check(cudaMemcpyAsync(c->part.p, part.data(), sizeof(int) * total, cudaMemcpyHostToDevice,
+                               s), "H2D pairs");
+    cuda_check(cudaMemcpyAsync(c->dr2.p, dr2.data(), sizeof(double) * total,
+                               cudaMemcpyHostToDevice, s), "H2D pairs");
+    cuda_check(cudaStreamSynchronize(s), "H2D pairs");
+}
+
+// IndexTable::assign_cells for every sightline: the segment of each pair's cell.
+const float2 *voronoi_cells(fsg_context *c, const Particles &p, const double *cofm, double box)
+{
+    const long long total = c->npairs;
+    const int nlos = c->nlos;
+    if (total <= 0)
+        return nullptr;
+    cudaStream_t s = c->stream;
+    sort_pairs_by_particle(c);
+    auto *seg = (float2 *)c->ensure(c->vseg, sizeof(float2) * total);
+    auto *scratch = (int *)c->ensure(c->vscratch,
+                                     sizeof(int) * voronoi_scratch_ints(total, nlos));
+    auto *dcofm = (double *)c->ensure(c->vcofm, sizeof(double) * 3 * nlos);
+    auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
+    cuda_check(cudaMemcpyAsync(dcofm, cofm, sizeof(double) * 3 * nlos, cudaMemcpyHostToDevice, s),
+               "H2D cofm");
+    cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
+    launch_voronoi_cells(p.pos, (const int *)c->part.p, (const long long *)c->off.p,
+                         c->tables.axis, dcofm, nlos, total, box, scratch, seg, err, s);
+    c->stats.gpu_launches += 10;
+    cuda_check(cudaGetLastError(), "Voronoi cells launch");
+    unsigned h_err = 0;
+    cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
+    cuda_check(cudaStreamSynchronize(s), "Voronoi cells");
+    if (h_err & DEVERR_VORONOI_CELL)
+        fail(FSG_ERR_VALUE, "a Voronoi cell's points along a sightline are not contiguous (the "
+                            "reference stops the program here: index_table.cpp:199-204)");
+    if (h_err)
+        fail(FSG_ERR_DEVICE, "Voronoi cells reported device error bits 0x%x (%s)", h_err,
+             deverr_text(h_err).c_str());
+    return seg;
+}
+
 void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, double box,
                      double velfac, double lambda, double gamma, double fosc, double amumass,
                      double tautail, const Particles &p, const int32_t *axis, const double *cofm,
@@ -643,7 +720,8 @@ void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, dou
     search_pairs(c, p, nlos);
     LineParams lp = make_line_params(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
                                      amumass, tautail);
-    deposit(c, lp, p, out, opt);
+    const float2 *seg = kernel == VORONOI ? voronoi_cells(c, p, cofm, box) : nullptr;
+    deposit(c, lp, p, out, opt, seg);
 }
 
 }  // namespace
@@ -739,7 +817,7 @@ int fsg_particle_interpolate_device(fsg_context *ctx, int compute_tau, int nbins
     try {
         if (!ctx)
             fail(FSG_ERR_VALUE, "ctx is NULL");
-        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm, true);
         Particles p{pos, vel, dens, temp, h, (long long)npart};
         run_interpolate(ctx, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
                         amumass, tautail, p, axis, cofm, nlos, out, opt);
@@ -758,7 +836,7 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
 {
     (void)atime;
     try {
-        validate_common(nbins, kernel, box, npart, nlos, axis, cofm);
+        validate_common(nbins, kernel, box, npart, nlos, axis, cofm, true);
         std::lock_guard<std::mutex> lock(g_default_mu);
         fsg_context *c = default_context();
         cudaStream_t s = c->stream;

@@ -124,6 +124,8 @@ __device__ T kern_frac(int kernel, T zlow, T zhigh, T smooth, T dr2, T zrange)
         return deltaz * total;
     }
     const T d = zhigh - zlow;
+    if (kernel == VORONOI)   // arepo_kern_frac, absorption.cpp:129-134: overlap length
+        return d > (T)0 ? d : (T)0;
     return (T)(3. / 4. / PI_D) * (d > (T)0 ? d : (T)0);
 }
 
@@ -318,6 +320,23 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
         in.ppos = in.dens = in.smooth = in.pvel = in.temp = 0.f;
         return in;
     }
+    if (pl.seg) {
+        // Voronoi mesh: the cell's segment ends stand in for dr2 and the
+        // smoothing length (part_int.cpp:42-43, 75-76)
+        const float2 g = pl.seg[e];
+        in.dr2 = (double)g.x;
+        in.smooth = g.y;
+        in.ppos = __ldg(&p.pos[3ll * ip + axis - 1]);
+        in.dens = __ldg(&p.dens[ip]);
+        if (tau) {
+            in.pvel = __ldg(&p.vel[3ll * ip + axis - 1]);
+            in.temp = __ldg(&p.temp[ip]);
+        } else {
+            in.pvel = 0.f;
+            in.temp = 0.f;
+        }
+        return in;
+    }
     const long long k = 3ll * ip + axis - 1;
     in.ppos = __ldg(&p.pos[k]);
     in.dens = __ldg(&p.dens[ip]);
@@ -353,17 +372,29 @@ struct Tau64 {
 
     __device__ __forceinline__ bool setup(const LineParams &lp, const PairInput &in)
     {
-        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-        if (hh2 - in.dr2 <= 0)
-            return false;   // absorption.cpp:232
+        const bool vor = lp.kernel == VORONOI;
+        double pos1 = (double)in.ppos;
+        if (vor) {
+            // absorption.cpp:221-227: segment [dr2, smooth] along the sightline
+            const double lim = 2 * lp.vbox / lp.velfac;
+            if (in.dr2 > lim || (double)in.smooth > lim)
+                return false;
+            pos1 = (in.dr2 + (double)in.smooth) / 2.;
+        } else {
+            const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+            if (hh2 - in.dr2 <= 0)
+                return false;   // absorption.cpp:232
+        }
         btherm = lp.bfac * sqrt((double)in.temp);
         half_b = btherm / 2.;
         inv_b = 1.0 / btherm;
-        vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
-        const double vdr2 = (lp.velfac * in.dr2) * lp.velfac;
+        vel = __dadd_rn(__dmul_rn(lp.velfac, pos1), (double)in.pvel);
+        const double vdr2 = vor ? lp.velfac * in.dr2 : (lp.velfac * in.dr2) * lp.velfac;
         const double vsmooth = lp.velfac * (double)in.smooth;
         aa = lp.voigt_fac / btherm;
-        const double vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
+        double vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
+        if (vor)   // singleabs.h:85-89
+            vhigh = (vdr2 > 0 && vsmooth > 0) ? (vsmooth - vdr2) / 2. : 0.;
         deltav = 2. * vhigh / NGRID;
 #pragma unroll
         for (int i = 1; i < NGRID; ++i) {
@@ -720,9 +751,15 @@ __device__ __forceinline__ double tau_pair_bound32(const Bound32 &k, const PairI
 // 7 x max|kernel weight| x max H, with H <= 1 for a >= 0.
 __device__ __forceinline__ double tau_pair_bound(const LineParams &lp, const PairInput &in)
 {
-    const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-    if (hh2 - in.dr2 <= 0)
-        return 0.0;
+    if (lp.kernel == VORONOI) {
+        const double lim = 2 * lp.vbox / lp.velfac;
+        if (in.dr2 > lim || (double)in.smooth > lim)
+            return 0.0;
+    } else {
+        const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
+        if (hh2 - in.dr2 <= 0)
+            return 0.0;
+    }
     const double btherm = lp.bfac * sqrt((double)in.temp);
     const double aa = lp.voigt_fac / btherm;
     const double hmax = aa >= 0 ? 1.0 : 2.0 * exp(aa * aa) + 1.0;
@@ -777,9 +814,18 @@ struct Colden {
     {
         pos1 = (double)in.ppos;
         const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
-        if (hh2 - in.dr2 <= 0)
-            return false;   // absorption.cpp:182
-        zrange = sqrt(hh2 - in.dr2);
+        if (lp.kernel == VORONOI) {
+            // absorption.cpp:170-186: segment [dr2, smooth], centre and half-length
+            const double lim = 2 * lp.vbox / lp.velfac;
+            if (in.dr2 > lim || (double)in.smooth > lim)
+                return false;
+            pos1 = (in.dr2 + (double)in.smooth) / 2.;
+            zrange = ((double)in.smooth - in.dr2) / 2.;
+        } else {
+            if (hh2 - in.dr2 <= 0)
+                return false;   // absorption.cpp:182
+            zrange = sqrt(hh2 - in.dr2);
+        }
         boxtokpc = btk;
         smooth = (double)in.smooth;
         dr2 = in.dr2;

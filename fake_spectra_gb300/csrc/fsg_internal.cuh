@@ -9,6 +9,7 @@
 //               128-bit fixed-point accumulators live in shared memory
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <string>
@@ -41,6 +42,7 @@ enum DeviceError : unsigned {
     DEVERR_WINDOW_LIMIT = 4u,     // a pixel window or sub-sample count beyond the limits below
     DEVERR_PAIR_COUNT = 8u,       // emit pass wrote fewer pairs of a sightline than counted
     DEVERR_PAIR_INDEX = 16u,      // a pair names a particle outside [0, n) (pair skipped)
+    DEVERR_VORONOI_CELL = 32u,    // a Voronoi cell's points along a sightline are not contiguous
 };
 
 // Names of the set bits, for error messages ("fixed-point overflow, ...").
@@ -48,9 +50,10 @@ inline std::string deverr_text(unsigned bits)
 {
     static const char *names[] = {"fixed-point overflow", "pair slot overflow",
                                   "window or sub-sample limit", "pair count mismatch",
-                                  "pair particle index out of range"};
+                                  "pair particle index out of range",
+                                  "non-contiguous Voronoi cell along a sightline"};
     std::string r;
-    for (int b = 0; b < 5; b++)
+    for (int b = 0; b < 6; b++)
         if (bits & (1u << b))
             r += (r.empty() ? "" : ", ") + std::string(names[b]);
     return r.empty() ? "unknown" : r;
@@ -124,6 +127,7 @@ struct PairLists {
     const long long *off;    // [L+1]
     const int *part;         // [P]
     const double *dr2;       // [P]
+    const float2 *seg = nullptr;   // [P] Voronoi cell segments (kernel 2), else null
 };
 
 // Host launchers (stream-ordered; no synchronisation inside).
@@ -163,6 +167,16 @@ void launch_colden_channels(const LineParams &lp, const LineTables &t, const Par
                             int *n_bad, unsigned *ticket, unsigned *dev_err,
                             unsigned long long *gacc, int precision, const ChannelPlan &plan,
                             int grid, cudaStream_t s);
+
+// Voronoi-mesh cells (fsg_voronoi.cu): seg[P] = the [left, right] segment
+// of each pair's cell along its sightline (IndexTable::assign_cells); the
+// pairs of a sightline must be in ascending particle order.  scratch holds
+// voronoi_scratch_ints(P, L) ints; cofm is a device copy (3L doubles).
+long long voronoi_scratch_ints(long long npairs, int nlos);
+void launch_voronoi_cells(const float *pos, const int *part, const long long *off,
+                          const int *axis, const double *cofm, int nlos, long long npairs,
+                          double box, int *scratch, float2 *seg, unsigned *dev_err,
+                          cudaStream_t s);
 
 // Flux statistics (fsg_flux.cu): deterministic two-pass reductions over tau.
 // out3 = {sum exp(-scale tau), sum tau exp(-scale tau), count} over tau <= thresh;

@@ -31,8 +31,11 @@ _p = ctypes.c_void_p
 
 
 def build_port(force=False):
-    """Compile the C restatement if its library is missing (or force)."""
-    if force or not os.path.exists(PORT_SO):
+    """Compile the C restatement if its library is missing or older than its
+    source (or force)."""
+    src = os.path.join(HERE, "fsg_oracle.c")
+    stale = os.path.exists(PORT_SO) and os.path.getmtime(PORT_SO) < os.path.getmtime(src)
+    if force or stale or not os.path.exists(PORT_SO):
         subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")],
                               stdout=subprocess.DEVNULL)
     return PORT_SO
@@ -93,6 +96,8 @@ class Oracle:
             L.fsgo_dawson.restype = _c_d
             L.fsgo_kern_frac.argtypes = [_c_int, _c_d, _c_d, _c_d, _c_d, _c_d]
             L.fsgo_kern_frac.restype = _c_d
+            L.fsgo_assign_cells.argtypes = [_p, _p, _c_int, _c_int, _p, _c_d, _p]
+            L.fsgo_assign_cells.restype = _c_int
         else:
             L.fsr_sph_cubic_kern_frac.argtypes = [_c_d] * 5
             L.fsr_sph_cubic_kern_frac.restype = _c_d
@@ -149,6 +154,18 @@ class Oracle:
         off = np.zeros(nlos + 1, dtype=np.int64)
         np.cumsum(counts, out=off[1:])
         return off, part[:total], dr2[:total]
+
+    def assign_cells(self, pos, part, axis, cofm3, box):
+        """Voronoi segments (float32, 2 per cell) of one sightline's cells."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        part = np.ascontiguousarray(part, dtype=np.int32)
+        cofm3 = np.ascontiguousarray(cofm3, dtype=np.float64)
+        seg = np.zeros(2 * max(len(part), 1), dtype=np.float32)
+        rc = self._fn("assign_cells")(_ptr(pos), _ptr(part), int(len(part)), int(axis),
+                                      _ptr(cofm3), float(box), _ptr(seg))
+        if rc != 0:
+            raise RuntimeError("non-contiguous Voronoi cell (the reference exits here)")
+        return seg[:2 * len(part)]
 
     def near_lines(self, cofm, axis, box, pos3, hh, cap=4096):
         cofm = np.ascontiguousarray(cofm, dtype=np.float64)

@@ -294,6 +294,17 @@ static double tophat_kern_frac(double zlow, double zhigh, double zrange)
     return 3. / 4. / O_PI * (d > 0. ? d : 0.);
 }
 
+/* absorption.cpp:129-134: the Voronoi cell's share of the pixel is the length
+ * of the overlap of the pixel with the cell's segment [-zrange, zrange]. */
+static double arepo_kern_frac(double zlow, double zhigh, double zrange)
+{
+    if (zlow < -zrange)
+        zlow = -zrange;
+    if (zhigh > zrange)
+        zhigh = zrange;
+    return zhigh - zlow > 0. ? zhigh - zlow : 0.;
+}
+
 /* absorption.cpp:136-148 (dispatch; unknown ids use the top hat) */
 double fsgo_kern_frac(int kernel, double zlow, double zhigh, double smooth, double dr2,
                       double zrange)
@@ -302,6 +313,8 @@ double fsgo_kern_frac(int kernel, double zlow, double zhigh, double smooth, doub
         return spline_kern_frac(fsgo_sph_cubic_kernel, zlow, zhigh, smooth, dr2, zrange);
     if (kernel == FSGO_SPH_QUINTIC)
         return spline_kern_frac(fsgo_sph_quintic_kernel, zlow, zhigh, smooth, dr2, zrange);
+    if (kernel == FSGO_VORONOI)
+        return arepo_kern_frac(zlow, zhigh, zrange);
     return tophat_kern_frac(zlow, zhigh, zrange);
 }
 
@@ -323,6 +336,10 @@ static void absorber_init(absorber_t *s, double btherm, double vdr2, double vsmo
     s->aa = aa;
     s->kernel = kernel;
     s->vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
+    /* singleabs.h:85-89: for the Voronoi mesh vdr2 and vsmooth are the cell's
+     * segment ends (velocity units) and the half-length is the node range */
+    if (kernel == FSGO_VORONOI)
+        s->vhigh = (vdr2 > 0 && vsmooth > 0) ? (vsmooth - vdr2) / 2. : 0;
     s->evals = 0;
 }
 
@@ -401,15 +418,24 @@ static int wrap_bin(int z, int nbins)
     return j;
 }
 
-/* absorption.cpp:167-210 (SPH kernels; the Voronoi branch is not restated) */
+/* absorption.cpp:167-210.  For the Voronoi mesh dr2 and smooth are the lower
+ * and upper ends of the cell's segment along the sightline. */
 static void add_colden(const line_t *l, double *colden, int nbins, double dr2, float dens,
                        float ppos, float smooth)
 {
-    const double pos1 = ppos;
-    const double hh2 = (double)(smooth * smooth); /* float product, as in the reference */
-    if (hh2 - dr2 <= 0)
-        return;
-    const double zrange = sqrt(hh2 - dr2);
+    double pos1 = ppos;
+    double zrange;
+    if (l->kernel == FSGO_VORONOI) {
+        if (dr2 > 2 * l->vbox / l->velfac || smooth > 2 * l->vbox / l->velfac)
+            return;
+        pos1 = (dr2 + smooth) / 2.;
+        zrange = (smooth - dr2) / 2.;
+    } else {
+        const double hh2 = (double)(smooth * smooth); /* float product, as in the reference */
+        if (hh2 - dr2 <= 0)
+            return;
+        zrange = sqrt(hh2 - dr2);
+    }
     const double boxtokpc = l->vbox / nbins / l->velfac;
     const int zlow = (int)floor((pos1 - zrange) / boxtokpc);
     const int zhigh = (int)ceil((pos1 + zrange) / boxtokpc);
@@ -424,14 +450,21 @@ static void add_colden(const line_t *l, double *colden, int nbins, double dr2, f
 static long long add_tau(const line_t *l, double *tau, int nbins, double dr2, float dens,
                          float ppos, float pvel, float temp, float smooth)
 {
-    const double pos1 = ppos;
+    double pos1 = ppos;
     const double btherm = l->bfac * sqrt((double)temp);
-    const double hh2 = (double)(smooth * smooth);
-    if (hh2 - dr2 <= 0)
-        return 0;
+    if (l->kernel == FSGO_VORONOI) {
+        if (dr2 > 2 * l->vbox / l->velfac || smooth > 2 * l->vbox / l->velfac)
+            return 0;
+        pos1 = (dr2 + smooth) / 2.;
+    } else {
+        const double hh2 = (double)(smooth * smooth);
+        if (hh2 - dr2 <= 0)
+            return 0;
+    }
     const double vel = l->velfac * pos1 + pvel;
     double val1 = l->velfac * dr2;
-    val1 *= l->velfac;
+    if (l->kernel != FSGO_VORONOI)
+        val1 *= l->velfac;
     absorber_t s;
     absorber_init(&s, btherm, val1, l->velfac * smooth, l->voigt_fac / btherm, l->kernel);
     const double bintov = l->vbox / nbins;
@@ -780,6 +813,65 @@ long long fsgo_near_particles(const float *pos, const float *h, long long npart,
 }
 
 /* ------------------------------------------------------------------ */
+/* Voronoi cells along a sightline, index_table.cpp:152-223            */
+/* ------------------------------------------------------------------ */
+#define O_RESO 0.1 /* index_table.h:8 */
+
+/* The sightline is sampled at N = int(box/RESO) points; each belongs to the
+ * nearest of the line's particles (periodic 3-D distance, the first in
+ * ascending particle order on a tie).  Cell k of the list gets the segment
+ * [seg[2k], seg[2k+1]] covered by its points (float, as the reference stores
+ * it), 3 box for cells with no point.  Returns 0, or -3 where the reference
+ * exits: a cell's points are not contiguous. */
+int fsgo_assign_cells(const float *pos, const int32_t *part, int ncells, int axis,
+                      const double *cofm3, double box, float *seg)
+{
+    for (int i = 0; i < 2 * ncells; ++i)
+        seg[i] = (float)(3 * box);
+    const int N = (int)(box / O_RESO);
+    const double reso = box / N;
+    const double yp = cofm3[axis % 3], zp = cofm3[(axis + 1) % 3];
+    for (int i = 0; i < N; ++i) {
+        const double xp = (i + 0.5) * reso;
+        double min_dist = box;
+        int min_ind = 0;
+        for (int k = 0; k < ncells; k++) {
+            const float *p3 = &pos[3 * (size_t)part[k]];
+            double dx = fabs(p3[axis - 1] - xp);
+            if (dx > box / 2.)
+                dx = box - dx;
+            double dy = fabs(p3[axis % 3] - yp);
+            if (dy > box / 2.)
+                dy = box - dy;
+            double dz = fabs(p3[(axis + 1) % 3] - zp);
+            if (dz > box / 2.)
+                dz = box - dz;
+            const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+            if (dist < min_dist) {
+                min_dist = dist;
+                min_ind = k;
+            }
+        }
+        /* the first cell wraps around the box: the rest of the line is its */
+        if (seg[2 * min_ind] < reso && xp > box / 2. + 0.5 * reso) {
+            seg[2 * min_ind] = (float)xp;
+            seg[2 * min_ind + 1] = (float)(seg[2 * min_ind + 1] + box);
+            break;
+        }
+        if (xp > 1.5 * reso + seg[2 * min_ind + 1])
+            return -3;
+        if (seg[2 * min_ind] > 2 * box)
+            seg[2 * min_ind] = (float)xp;
+        seg[2 * min_ind + 1] = (float)xp;
+    }
+    for (int k = 0; k < ncells; ++k) {
+        seg[2 * k] = (float)(seg[2 * k] - 0.5 * reso);
+        seg[2 * k + 1] = (float)(seg[2 * k + 1] + 0.5 * reso);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* ParticleInterp, part_int.cpp:20-84                                  */
 /* ------------------------------------------------------------------ */
 int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box, double velfac,
@@ -790,31 +882,51 @@ int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box
                               double *out, long long *evals)
 {
     (void)atime;
-    if (kernel == FSGO_VORONOI)
-        return -2;
     memset(out, 0, sizeof(double) * (size_t)nlos * (size_t)nbins);
     csr_t c;
     build_csr(pos, h, npart, axis, cofm, nlos, box, &c);
     line_t l;
     line_init(&l, lambda, gamma, fosc, amumass, velfac, box, kernel, tautail);
     long long nev = 0;
+    int failed = 0;
     int nth = fsgo_get_threads();
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nth) reduction(+ : nev)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth) reduction(+ : nev, failed)
     for (int i = 0; i < nlos; i++) {
         const int ax = axis[i];
         double *row = &out[(size_t)i * nbins];
+        const long long m = c.off[i + 1] - c.off[i];
+        float *seg = NULL;
+        if (kernel == FSGO_VORONOI) {
+            seg = (float *)malloc(sizeof(float) * 2 * (m > 0 ? m : 1));
+            if (fsgo_assign_cells(pos, &c.part[c.off[i]], (int)m, ax, &cofm[3 * (size_t)i], box,
+                                  seg) != 0) {
+                failed++;
+                free(seg);
+                continue;
+            }
+        }
         for (long long e = c.off[i]; e < c.off[i + 1]; e++) {
             const int ip = c.part[e];
             const float ppos = pos[3 * (size_t)ip + ax - 1];
+            /* the Voronoi mesh passes its segment ends for dr2 and smooth */
+            const double d2 = seg ? (double)seg[2 * (e - c.off[i])] : c.dr2[e];
+            const float sm = seg ? seg[2 * (e - c.off[i]) + 1] : h[ip];
             if (compute_tau)
-                nev += add_tau(&l, row, nbins, c.dr2[e], dens[ip], ppos,
-                               vel[3 * (size_t)ip + ax - 1], temp[ip], h[ip]);
+                nev += add_tau(&l, row, nbins, d2, dens[ip], ppos, vel[3 * (size_t)ip + ax - 1],
+                               temp[ip], sm);
             else
-                add_colden(&l, row, nbins, c.dr2[e], dens[ip], ppos, h[ip]);
+                add_colden(&l, row, nbins, d2, dens[ip], ppos, sm);
         }
+        free(seg);
     }
     if (evals)
         *evals = nev;
+    if (failed) {
+        free(c.off);
+        free(c.part);
+        free(c.dr2);
+        return -3;
+    }
     free(c.off);
     free(c.part);
     free(c.dr2);

@@ -42,6 +42,12 @@ long long fsgo_near_particles(const float *pos, const float *h, long long npart,
                               const int32_t *axis, const double *cofm, int nlos, double box,
                               long long *counts, int32_t *part, double *dr2, long long cap);
 
+/* Voronoi segments of one sightline's cells (index_table.cpp:152-223):
+ * part[ncells] in ascending order, cofm3 the sightline position; seg[2*ncells].
+ * Returns 0, or -3 where the reference exits (non-contiguous cell). */
+int fsgo_assign_cells(const float *pos, const int32_t *part, int ncells, int axis,
+                      const double *cofm3, double box, float *seg);
+
 /* Lines near one particle (index_table.cpp:117-127); returns count. */
 int fsgo_near_lines(const double *cofm, const int32_t *axis, int nlos, double box,
                     const float *pos3, float hh, int32_t *lines, double *dr2, int cap);

@@ -5,7 +5,7 @@ reference C++ path (oracle/build_ref.sh -> oracle/_ref/libfsref.so), feeds it
 small seeded inputs and stores inputs + reference outputs as .npz files.  The
 fixtures then travel with the tests to machines without the reference.
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py [/root/reference [voronoi]]
 """
 import os
 import sys
@@ -73,11 +73,45 @@ def subsample(w, npart, nlos, seed):
     return idx, lidx
 
 
-def main(ref_root="/root/reference"):
+def voronoi_fixture(R, seed=21):
+    """Random cells in a 1 Mpc/h box, one wrapping first cell (a particle at
+    the box edge on a sightline), tau and column density with kernel 2 from the
+    reference's assign_cells path (index_table.cpp:152-223)."""
+    rng = np.random.default_rng(seed)
+    box = 1000.0
+    n = 2500
+    pos = rng.uniform(0, box, size=(n, 3)).astype(np.float32)
+    nl = 12
+    axis = rng.integers(1, 4, nl).astype(np.int32)
+    cofm = rng.uniform(0, box, size=(nl, 3))
+    # sightline 0 (axis 1): a dense particle right next to it at the box edge
+    axis[0] = 1
+    pos[0] = [box - 0.7, cofm[0, 1] + 0.3, cofm[0, 2] - 0.2]
+    vel = (30 * rng.standard_normal((n, 3))).astype(np.float32)
+    dens = (rng.lognormal(0, 1, n) * 3e11).astype(np.float32)
+    temp = (1e4 * rng.lognormal(0, 0.3, n)).astype(np.float32)
+    hh = (60.0 * rng.lognormal(0, 0.2, n)).astype(np.float32)
+    _, _, velfac = synth.cosmology()
+    nbins = int(box * velfac / 0.5)
+    out = dict(pos=pos, vel=vel, dens=dens, temp=temp, hh=hh, axis=axis, cofm=cofm, box=box,
+               nbins=nbins, velfac=velfac)
+    for t in (synth.LYA, synth.CIV):
+        for ct in (0, 1):
+            out["%s_%s" % ("tau" if ct else "colden", t.name)] = R.particle_interpolate(
+                ct, nbins, 2, box, velfac, 0.25, t.lambda_cm, t.gamma, t.fosc, t.amumass, 1e-7,
+                pos, vel, dens, temp, hh, axis, cofm)
+    return out
+
+
+def main(ref_root="/root/reference", only=None):
     oracle.build_ref(ref_root)
     R = oracle.ref()
     if R is None:
         raise SystemExit("reference sources not found under %s" % ref_root)
+    if only in (None, "voronoi"):
+        np.savez_compressed(os.path.join(HERE, "voronoi.npz"), **voronoi_fixture(R))
+        if only:
+            return
 
     # 1. reference IndexTable fixture
     axis, cofm, pos, hh, box = index_fixture()

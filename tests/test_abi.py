@@ -129,11 +129,20 @@ def test_axis_out_of_range(lib):
         call(a)
 
 
-def test_voronoi_not_implemented(lib):
+def test_voronoi_rejected_where_unsupported(lib):
+    """kernel=2 runs through the interpolation entry points (GPU tests); the
+    no-allocation entry point rejects it before touching the device."""
+    import ctypes
+    from fake_spectra_gb300 import _lib
     a = _args()
-    a[2] = 2
+    ptr = lambda x: np.ascontiguousarray(x).ctypes.data_as(ctypes.c_void_p)
+    out = np.zeros((2, 16))
+    eb = _lib.errbuf()
+    rc = _lib.load().fsg_particle_interpolate_noalloc(
+        1, 16, 2, *[float(v) for v in a[3:11]], ptr(a[11]), ptr(a[12]), ptr(a[13]), ptr(a[14]),
+        ptr(a[15]), len(a[11]), ptr(a[16]), ptr(a[17]), len(a[16]), ptr(out), 0, None, eb, 512)
     with pytest.raises(NotImplementedError):
-        call(a)
+        _lib.raise_for(rc, eb.value.decode())
 
 
 def test_empty_outputs_need_no_device():
