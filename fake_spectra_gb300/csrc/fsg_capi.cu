@@ -684,6 +684,9 @@ const float2 *voronoi_cells(fsg_context *c, const Particles &p, const double *co
     const int nlos = c->nlos;
     if (total <= 0)
         return nullptr;
+    if (!(box / 0.1 < 1e9))
+        fail(FSG_ERR_VALUE, "box %g too large for the Voronoi sightline grid (0.1 kpc/h points)",
+             box);
     cudaStream_t s = c->stream;
     sort_pairs_by_particle(c);
     auto *seg = (float2 *)c->ensure(c->vseg, sizeof(float2) * total);
