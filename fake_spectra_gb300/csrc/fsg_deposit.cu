@@ -1949,14 +1949,19 @@ void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 {
     const size_t cap = (size_t)(max_smem_optin() - STATIC_SMEM_RESERVE);
     if (cfg.precision == 1) {
-        // staged pairs: 32 per warp, or 16 to keep the accumulators on chip
-        for (int chunk : {32, 16}) {
+        // staged pairs per warp: 8 for tau (finer chunks balance the warps
+        // better at the end of a sightline, where pair costs differ most), 32
+        // (or 16 to keep the accumulators on chip) for the column density
+        const int first = compute_tau ? 8 : 32;
+        for (int chunk : {first, 16, 8}) {
+            if (chunk > first)
+                continue;
             cfg.chunk = chunk;
             cfg.smem_mode = 1;
             if (deposit_smem_bytes(cfg, compute_tau, nbins) <= cap)
                 return;
         }
-        cfg.chunk = 32;
+        cfg.chunk = first;
         cfg.smem_mode = 0;
         return;
     }
@@ -1966,7 +1971,7 @@ void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 
 int deposit_max_smem_bins(int compute_tau, int precision, int threads)
 {
-    const size_t stage = (size_t)(threads / 32) * 16 * stage_pair_bytes(compute_tau, precision);
+    const size_t stage = (size_t)(threads / 32) * 8 * stage_pair_bytes(compute_tau, precision);
     return (int)(((size_t)(max_smem_optin() - STATIC_SMEM_RESERVE) - stage) / 16);
 }
 
