@@ -100,7 +100,8 @@ def dist_setup():
         backend = "nccl" if torch.cuda.is_available() else "gloo"
         if backend == "nccl":
             torch.cuda.set_device(local)
-        dist.init_process_group(backend)
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
     return rank, world, local
 
 
