@@ -51,9 +51,10 @@ F_EVAL = 32
 # (7 evaluations): 20/7 each.
 FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 # DRAM traffic of the FP32 deposit from one ncu capture of the 192^3 slice of
-# the 256^3 workload (profiles/deposit_fp32_config1_192cube.md): 3.745 GB read
-# for 7545574 pairs, 0.1905 GB written for 3600 x 6691 pixels; scaled to a
-# launch by pairs (reads) and output pixels (writes).
+# the 256^3 workload (dram__bytes_read.sum + dram__bytes_write.sum, kept with
+# the profile summaries): 3.745 GB read for 7545574 pairs, 0.1905 GB written for
+# 3600 x 6691 pixels; scaled to a launch by pairs (reads) and output pixels
+# (writes).
 TRAFFIC_READ_PER_PAIR = 3.745174e9 / 7545574
 TRAFFIC_WRITE_PER_PIXEL = 0.19050368e9 / (3600 * 6691)
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
