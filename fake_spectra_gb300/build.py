@@ -72,7 +72,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

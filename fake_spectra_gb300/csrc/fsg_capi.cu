@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -619,6 +620,72 @@ void ctx_init(fsg_context *c, int device)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
 }
 
+// Device-to-host copy by a kernel that stores straight into the caller's host
+// array, for devices that access pageable host memory coherently (GB300 with
+// Grace over NVLink-C2C); the pages are resident by then (PreTouch), so the
+// stores run at link bandwidth instead of through the driver's staging copy.
+__global__ void copy_to_host_kernel(const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                    size_t n2)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride)
+        dst[i] = src[i];
+}
+
+void copy_to_host(fsg_context *c, void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device);
+    cudaPointerAttributes pa{};
+    const bool plain_host = cudaPointerGetAttributes(&pa, dst) == cudaSuccess &&
+                            pa.type == cudaMemoryTypeUnregistered;
+    cudaGetLastError();   // an unregistered pointer may leave an error behind
+    if (pageable && plain_host && bytes >= (64u << 20) && ((uintptr_t)dst % 16) == 0 &&
+        ((uintptr_t)src % 16) == 0 && bytes % 16 == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        copy_to_host_kernel<<<sms * 8, 256, 0, s>>>((const double2 *)src, (double2 *)dst,
+                                                    bytes / 16);
+        c->stats.gpu_launches++;
+        cuda_check(cudaGetLastError(), "copy to host launch");
+        return;
+    }
+    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), "D2H");
+}
+
+// Writes zeros over a caller's host output from a few threads while the GPU
+// works.  A fresh allocation (NumPy's zeros, calloc) has no pages yet; without
+// this the device-to-host copy at the end of the call faults them in one by
+// one, which on this machine costs more than the copy itself.
+class PreTouch {
+  public:
+    PreTouch(void *p, size_t bytes)
+    {
+        if (!p || bytes < (64u << 20))
+            return;
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t n = std::min<size_t>(8, std::max<size_t>(1, hw / 2));
+        const size_t chunk = (bytes / n + 4095) & ~(size_t)4095;
+        for (size_t i = 0; i < n; i++) {
+            const size_t off = i * chunk;
+            if (off >= bytes)
+                break;
+            const size_t len = std::min(chunk, bytes - off);
+            threads_.emplace_back([p, off, len] { memset((char *)p + off, 0, len); });
+        }
+    }
+    void wait()
+    {
+        for (auto &t : threads_)
+            t.join();
+        threads_.clear();
+    }
+    ~PreTouch() { wait(); }
+
+  private:
+    std::vector<std::thread> threads_;
+};
+
 // The per-device context of the host-pointer entry points (created on first
 // use; the caller holds g_default_mu).
 fsg_context *default_context()
@@ -859,10 +926,12 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         p.temp = compute_tau ? up(c->temp, temp, n1) : nullptr;
         const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
         double *dout = (double *)c->ensure(c->out, nout);
+        PreTouch touch(out, nout);
         run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
                         tautail, p, axis, cofm, nlos, dout, opt);
+        touch.wait();
         if (nout)
-            cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
+            copy_to_host(c, out, dout, nout, s);
         cuda_check(cudaStreamSynchronize(s), "D2H");
         return FSG_OK;
     } catch (const FsgError &e) {

@@ -58,3 +58,19 @@ def test_pair_count_consistent(ctx, w256):
     n = I.build_pairs(ctx, w.box, w.pos, w.hh, w.axis, w.cofm)
     I.particle_interpolate_device(ctx, *w.call_args(synth.LYA, 1), precision="fp32")
     assert ctx.stats()["npairs"] == n > 1e6
+
+
+def test_host_api_large_output(ctx, w256):
+    """The host-pointer entry point with a 193 MB output (written to the caller's
+    fresh NumPy array by the copy kernel where the device can store to pageable
+    host memory) equals the device entry point."""
+    import torch
+    from fake_spectra_gb300 import interp as I
+    from fake_spectra_gb300._spectra_priv import _Particle_Interpolate
+    w = w256
+    a = list(w.call_args(synth.LYA, 1))
+    dev = I.particle_interpolate_device(ctx, *a, precision="fp32").cpu().numpy()
+    h = [x.cpu().numpy() for x in (w.pos, w.vel, w.dens["HI"], w.temp, w.hh)]
+    host = _Particle_Interpolate(*a[:11], *h, w.axis, w.cofm, precision="fp32")
+    assert host.nbytes >= 64 << 20
+    np.testing.assert_array_equal(host, dev)
