@@ -620,39 +620,6 @@ void ctx_init(fsg_context *c, int device)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
 }
 
-// Device-to-host copy by a kernel that stores straight into the caller's host
-// array, for devices that access pageable host memory coherently (GB300 with
-// Grace over NVLink-C2C); the pages are resident by then (PreTouch), so the
-// stores run at link bandwidth instead of through the driver's staging copy.
-__global__ void copy_to_host_kernel(const double2 *__restrict__ src, double2 *__restrict__ dst,
-                                    size_t n2)
-{
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride)
-        dst[i] = src[i];
-}
-
-void copy_to_host(fsg_context *c, void *dst, const void *src, size_t bytes, cudaStream_t s)
-{
-    int pageable = 0;
-    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device);
-    cudaPointerAttributes pa{};
-    const bool plain_host = cudaPointerGetAttributes(&pa, dst) == cudaSuccess &&
-                            pa.type == cudaMemoryTypeUnregistered;
-    cudaGetLastError();   // an unregistered pointer may leave an error behind
-    if (pageable && plain_host && bytes >= (64u << 20) && ((uintptr_t)dst % 16) == 0 &&
-        ((uintptr_t)src % 16) == 0 && bytes % 16 == 0) {
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-        copy_to_host_kernel<<<sms * 8, 256, 0, s>>>((const double2 *)src, (double2 *)dst,
-                                                    bytes / 16);
-        c->stats.gpu_launches++;
-        cuda_check(cudaGetLastError(), "copy to host launch");
-        return;
-    }
-    cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), "D2H");
-}
-
 // Writes zeros over a caller's host output from a few threads while the GPU
 // works.  A fresh allocation (NumPy's zeros, calloc) has no pages yet; without
 // this the device-to-host copy at the end of the call faults them in one by
@@ -931,7 +898,7 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
                         tautail, p, axis, cofm, nlos, dout, opt);
         touch.wait();
         if (nout)
-            copy_to_host(c, out, dout, nout, s);
+            cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "D2H");
         return FSG_OK;
     } catch (const FsgError &e) {

@@ -61,9 +61,9 @@ def test_pair_count_consistent(ctx, w256):
 
 
 def test_host_api_large_output(ctx, w256):
-    """The host-pointer entry point with a 193 MB output (written to the caller's
-    fresh NumPy array by the copy kernel where the device can store to pageable
-    host memory) equals the device entry point."""
+    """The host-pointer entry point with a 193 MB output (its fresh NumPy array
+    pre-faulted by host threads during the GPU work) equals the device entry
+    point."""
     import torch
     from fake_spectra_gb300 import interp as I
     from fake_spectra_gb300._spectra_priv import _Particle_Interpolate
