@@ -68,6 +68,21 @@ def measured_hbm_gbs():
         return None
 
 
+def search_roofline(npart, npairs, nlos, ms):
+    """HBM view of the sightline search (particle sort + count + emit): the
+    algorithmic bytes are the particle stream and the pair lists.  Sort: read
+    pos (12 B), write the cell key (4 B), read the key and write the order
+    (8 B); count and emit: read the order (4 B), pos (12 B) and h (4 B) each;
+    emit: write 12 B per pair; offsets 8 B per sightline."""
+    algo = npart * (12 + 4 + 8 + 2 * (4 + 12 + 4)) + npairs * 12 + nlos * 8
+    hbm = measured_hbm_gbs()
+    achieved = algo / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm if hbm else None, "bytes": algo,
+            "note": "the search is limited by the FP64 predicate and the cell walk, not by "
+                    "HBM (16 B of particle data per particle per pass)"}
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -314,6 +329,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "phases_ms": {"search": sum(search_ms) / len(search_ms), "deposit": dep_mean},
+        "search_roofline": search_roofline(w.npart, npairs, w.nlos,
+                                           sum(search_ms) / len(search_ms)),
         "roofline": {"bound": "fp32-pipe", "kernel": "deposit_kernel<tau, FP32>",
                      "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32,
