@@ -79,8 +79,10 @@ def search_roofline(npart, npairs, nlos, ms):
     achieved = algo / (ms * 1e-3) / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm if hbm else None, "bytes": algo,
-            "note": "the search is limited by the FP64 predicate and the cell walk, not by "
-                    "HBM (16 B of particle data per particle per pass)"}
+            "note": "the search is limited by the cell walk (latency of the dependent cell "
+                    "and sightline loads), not by HBM (16 B of particle data per particle "
+                    "per pass); the FP64 predicate runs only on the thin shell the float "
+                    "tests cannot decide"}
 
 
 def parse_args():

@@ -212,7 +212,7 @@ void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int n
     }
     std::vector<float4> pk(nlos);
     for (int i = 0; i < nlos; i++)
-        pk[i] = pack_line(key[i], second[i], axis[i]);
+        pk[i] = pack_line(key[i], second[i], axis[i], box);
     void *dk = c->ensure(c->key, sizeof(double) * nlos);
     void *ds = c->ensure(c->second, sizeof(double) * nlos);
     void *da = c->ensure(c->axis, sizeof(int) * nlos);
@@ -230,8 +230,7 @@ void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int n
     t.second = (const double *)ds;
     t.axis = (const int *)da;
     t.pack = (const float4 *)dp;
-    t.box_f = (float)box;
-    t.pre_eps = prefilter_eps(box);
+    set_float_box(t, box);
     c->nlos = nlos;
 }
 

@@ -33,11 +33,12 @@ struct Window {   // first-coordinate window of one table for one particle
     bool nowrap;
 };
 
-__device__ __forceinline__ Window make_window(float first, float hh, double box)
+__device__ __forceinline__ Window make_window(float first, float hh, const LineTables &t)
 {
     Window w;
+    const double box = t.box;
     float ffp = __fadd_rn(first, hh);
-    if ((double)ffp > box)
+    if (ffp >= t.box_up)   // (double)ffp > box
         ffp = (float)__dsub_rn((double)ffp, box);
     float ffm = __fsub_rn(first, hh);
     if (ffm < 0.0f)
@@ -82,27 +83,56 @@ __device__ __forceinline__ double calc_dr2(double d1, double d2, double box)
     return __dadd_rn(dr2, __dmul_rn(dr, dr));
 }
 
+// Sufficient float conditions for the window tests.  Rounding to float is
+// monotone, so for a float bound b and the float copy k = rn(key):
+// k > b implies key > b and k < b implies key < b.
+__device__ __forceinline__ bool window_holds(const Window &w, float k)
+{
+    return w.nowrap ? (k > w.ffm && k < w.ffp) : (k < w.ffp || k > w.ffm);
+}
+
+__device__ __forceinline__ bool second_holds(float second, float k, float hh)
+{
+    return k > __fsub_rn(second, hh) && k < __fadd_rn(second, hh);
+}
+
 // The reference predicate for (particle, line).  `first` is the particle's
 // coordinate for the table the line is in; pos3 the particle position.
-// A float prefilter rejects candidates whose minimum-image distance exceeds
-// hh by more than the float error bound (pre_eps, 4 ulp of the box) before the
-// exact FP64 test: a strict superset of the accepted set, so the result is
-// unchanged while most candidates cost FP32 work only (FP64 runs at 1/64 of the
-// FP32 rate on this GPU).
+// Most candidates are decided in FP32 (FP64 runs at 1/64 of the FP32 rate on
+// this GPU):
+//   * reject: the float minimum-image distance exceeds hh by more than its
+//     error bound (pre_eps, 4 ulp of the box), a strict superset test;
+//   * accept: the line's float copies lie within half an ulp of the box of the
+//     double values (pack.w), both distances stay below 0.49 box (no minimum
+//     image in calc_dr2), the upper bound of dr2 with every rounding of the
+//     float and double arithmetic (relative 2e-7, absolute pre_eps per
+//     coordinate) is below hh*hh by a relative 5e-6, and both windows hold by
+//     window_holds/second_holds, so the exact test below would return true.
+// The rest (the thin shell |dr| ~ hh, sightlines near the periodic boundary,
+// coordinates outside the box) takes the exact FP64 test.  The accepted set is
+// the reference's; dr2 itself is computed by pair_dr2_kernel.
 __device__ __forceinline__ bool accept(const LineTables &t, int line, const Window &w,
-                                       float first, const float *pos3, float hh, double *dr2_out)
+                                       float first, const float *pos3, float hh)
 {
     const float4 pk = __ldg(&t.pack[line]);
     const int ax = __float_as_int(pk.z);
     const float second = (ax == 3) ? pos3[1] : pos3[2];
     {
-        float d1 = fabsf(first - pk.x), d2 = fabsf(second - pk.y);
+        const float d1 = fabsf(first - pk.x), d2 = fabsf(second - pk.y);
         if (d1 <= t.box_f && d2 <= t.box_f && hh > 0.0f) {
-            d1 = fminf(d1, t.box_f - d1);
-            d2 = fminf(d2, t.box_f - d2);
+            const float m1 = fminf(d1, t.box_f - d1), m2 = fminf(d2, t.box_f - d2);
             const float lim = hh + t.pre_eps;
-            if (fmaf(d1, d1, d2 * d2) > lim * lim * 1.000001f)
+            if (fmaf(m1, m1, m2 * m2) > lim * lim * 1.000001f)
                 return false;
+            if (pk.w != 0.0f) {
+                const float a = fmaf(d1, 1.0000005f, t.pre_eps);
+                const float b = fmaf(d2, 1.0000005f, t.pre_eps);
+                const float half_in = 0.49f * t.box_f;
+                if (a <= half_in && b <= half_in &&
+                    fmaf(a, a, __fmul_rn(b, b)) <= __fmul_rn(__fmul_rn(hh, hh), 0.999995f) &&
+                    window_holds(w, pk.x) && second_holds(second, pk.y, hh))
+                    return true;
+            }
         }
     }
     const double key = t.key[line];
@@ -113,11 +143,7 @@ __device__ __forceinline__ bool accept(const LineTables &t, int line, const Wind
         return false;
     const double dr2 = calc_dr2(__dsub_rn((double)first, key), __dsub_rn((double)second, lproj2),
                                 t.box);
-    if (dr2 <= (double)__fmul_rn(hh, hh)) {
-        *dr2_out = dr2;
-        return true;
-    }
-    return false;
+    return dr2 <= (double)__fmul_rn(hh, hh);
 }
 
 // Coordinates of the particle in an axis group: (table first, cell second).
@@ -135,22 +161,25 @@ __device__ __forceinline__ void group_coords(int g, const float *pos3, float *fi
     }
 }
 
-// Cell range [c0, c0+cn) (mod nc) covering coordinate c +- reach.
-__device__ __forceinline__ void cell_range(double c, double reach, const LineGroup &G, int *c0,
-                                           int *cn)
+// Cell range [c0, c0+cn) (mod nc) covering coordinate c +- r, in float: the
+// rounding of (c -+ r) * inv_cw is below 1e-3 of a cell for |c| <= 4 box and
+// nc <= 1024, inside the margin the caller adds to r.  Coordinates further
+// out (or a range as wide as the grid) take every cell.
+__device__ __forceinline__ void cell_range(float c, float r, const LineGroup &G, float box_f,
+                                           int *c0, int *cn)
 {
-    double lo = floor((c - reach) * G.inv_cw);
-    double hi = floor((c + reach) * G.inv_cw);
-    double n = hi - lo + 1.0;
-    if (!(n < (double)G.nc)) {
+    const float lo = floorf((c - r) * G.inv_cw_f);
+    const float hi = floorf((c + r) * G.inv_cw_f);
+    const float n = hi - lo + 1.0f;
+    if (!(fabsf(c) <= 4.0f * box_f) || !(n < (float)G.nc)) {
         *c0 = 0;
         *cn = G.nc;
         return;
     }
-    long long l = (long long)lo % G.nc;
+    int l = (int)lo % G.nc;   // |lo| <= 4.5 nc + 1 here
     if (l < 0)
         l += G.nc;
-    *c0 = (int)l;
+    *c0 = l;
     *cn = (int)n;
 }
 
@@ -167,9 +196,9 @@ __device__ __forceinline__ void for_each_pair(const LineTables &t, const float *
         return;   // dr2 <= NaN is never true
     Window wmain, wxx;
     if (t.n_main)
-        wmain = make_window(pos3[0], hh, t.box);
+        wmain = make_window(pos3[0], hh, t);
     if (t.n_xx)
-        wxx = make_window(pos3[1], hh, t.box);
+        wxx = make_window(pos3[1], hh, t);
     if (!(hh > 0.0f) || isinf(hh)) {
         // hh <= 0 with every coordinate inside [0, box]: the first-coordinate
         // window is empty (hh == 0) or second_close needs ffm < lproj2 < ffp with
@@ -183,15 +212,15 @@ __device__ __forceinline__ void for_each_pair(const LineTables &t, const float *
             return;
         for (int l = 0; l < t.nlos; l++) {
             const bool xx = (t.axis[l] == 1);
-            double dr2;
-            if (accept(t, l, xx ? wxx : wmain, xx ? pos3[1] : pos3[0], pos3, hh, &dr2))
-                visit(l, dr2);
+            if (accept(t, l, xx ? wxx : wmain, xx ? pos3[1] : pos3[0], pos3, hh))
+                visit(l);
         }
         return;
     }
-    // Safety margin: relative 1e-6 of hh plus 1e-6 of a cell covers every
-    // rounding in the accept test and in the cell assignment of the lines.
-    const double reach = (double)hh * (1.0 + 1e-6);
+    // Safety margin: relative 1e-5 of hh plus 2e-2 of a cell covers every
+    // rounding in the accept test, in the float cell range and in the cell
+    // assignment of the lines.
+    const float reach = hh * 1.00001f;
 #pragma unroll 1
     for (int g = 0; g < 3; g++) {
         const LineGroup &G = t.g[g];
@@ -201,10 +230,10 @@ __device__ __forceinline__ void for_each_pair(const LineTables &t, const float *
         group_coords(g, pos3, &f, &s);
         if (!isfinite(f) || !isfinite(s))
             continue;   // with finite hh, a non-finite coordinate never passes dr2 <= hh^2
-        const double r = reach + 1e-6 * G.cw;
+        const float r = fmaf(0.02f, G.cw_f, reach);
         int a0, an, b0, bn;
-        cell_range((double)f, r, G, &a0, &an);
-        cell_range((double)s, r, G, &b0, &bn);
+        cell_range(f, r, G, t.box_f, &a0, &an);
+        cell_range(s, r, G, t.box_f, &b0, &bn);
         const Window &w = (g == 0) ? wxx : wmain;
         for (int ia = 0; ia < an; ia++) {
             int ca = a0 + ia;
@@ -218,9 +247,8 @@ __device__ __forceinline__ void for_each_pair(const LineTables &t, const float *
                 const int e1 = G.cell_start[cell + 1];
                 for (int e = G.cell_start[cell]; e < e1; e++) {
                     const int l = G.cell_line[e];
-                    double dr2;
-                    if (accept(t, l, w, f, pos3, hh, &dr2))
-                        visit(l, dr2);
+                    if (accept(t, l, w, f, pos3, hh))
+                        visit(l);
                 }
             }
         }
@@ -248,7 +276,7 @@ __global__ void count_pairs_kernel(LineTables t, Particles p, const int *perm,
         float pos3[3], hh;
         load_particle(p, i, pos3, &hh);
         int found = 0;
-        for_each_pair(t, pos3, hh, [&](int l, double) {
+        for_each_pair(t, pos3, hh, [&](int l) {
             const unsigned am = __activemask();
             const unsigned g = __match_any_sync(am, l);
             if (lane == __ffs(g) - 1)
@@ -261,8 +289,7 @@ __global__ void count_pairs_kernel(LineTables t, Particles p, const int *perm,
 }
 
 __global__ void emit_pairs_kernel(LineTables t, Particles p, const int *perm, const long long *off,
-                                  unsigned long long *cursor, int *part, double *dr2,
-                                  unsigned *dev_err)
+                                  unsigned long long *cursor, int *part, unsigned *dev_err)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
@@ -271,7 +298,7 @@ __global__ void emit_pairs_kernel(LineTables t, Particles p, const int *perm, co
         const long long i = perm ? (long long)perm[k] : k;
         float pos3[3], hh;
         load_particle(p, i, pos3, &hh);
-        for_each_pair(t, pos3, hh, [&](int l, double d) {
+        for_each_pair(t, pos3, hh, [&](int l) {
             const unsigned am = __activemask();
             const unsigned g = __match_any_sync(am, l);
             const int leader = __ffs(g) - 1;
@@ -280,13 +307,38 @@ __global__ void emit_pairs_kernel(LineTables t, Particles p, const int *perm, co
                 base = atomicAdd(&cursor[l], (unsigned long long)__popc(g));
             base = __shfl_sync(g, base, leader);
             const long long slot = off[l] + (long long)base + __popc(g & below);
-            if (slot < off[l + 1]) {
+            if (slot < off[l + 1])
                 part[slot] = (int)i;
-                dr2[slot] = d;
-            } else {
+            else
                 atomicOr(dev_err, (unsigned)DEVERR_PAIR_SLOT);
-            }
         });
+    }
+}
+
+// dr2 of every pair (calc_dr2, index_table.cpp:70-87): one CTA per sightline,
+// its pairs across the threads, so the FP64 arithmetic runs with full warps.
+// The emit pass accepted these pairs with the same function of the same
+// values.  A slot the emit pass left unwritten (a count mismatch, flagged by
+// check_emit_kernel) holds no particle index to trust: it is range-checked.
+__global__ void __launch_bounds__(256) pair_dr2_kernel(LineTables t, const float *pos,
+                                                       long long npart, const long long *off,
+                                                       const int *part, double *dr2,
+                                                       unsigned *dev_err)
+{
+    const int l = blockIdx.x;
+    const int ax = t.axis[l];
+    const double key = t.key[l], lproj2 = t.second[l];
+    const int fi = (ax == 1) ? 1 : 0, si = (ax == 3) ? 1 : 2;
+    const long long e1 = off[l + 1];
+    for (long long e = off[l] + threadIdx.x; e < e1; e += blockDim.x) {
+        const int i = part[e];
+        if (i < 0 || (long long)i >= npart) {
+            atomicOr(dev_err, (unsigned)DEVERR_PAIR_INDEX);
+            dr2[e] = 0.0;
+            continue;
+        }
+        const float f = __ldg(&pos[3 * (size_t)i + fi]), s = __ldg(&pos[3 * (size_t)i + si]);
+        dr2[e] = calc_dr2(__dsub_rn((double)f, key), __dsub_rn((double)s, lproj2), t.box);
     }
 }
 
@@ -395,7 +447,7 @@ __global__ void flag_near_kernel(LineTables t, Particles p, const int *perm, uns
         float pos3[3], hh;
         load_particle(p, i, pos3, &hh);
         int found = 0;
-        for_each_pair(t, pos3, hh, [&](int, double) { found = 1; });
+        for_each_pair(t, pos3, hh, [&](int) { found = 1; });
         flag[i] = (unsigned char)found;
     }
 }
@@ -503,8 +555,9 @@ void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
 {
     if (p.n == 0)
         return;
-    emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, off, cursor, part, dr2,
-                                                       dev_err);
+    emit_pairs_kernel<<<search_grid(p.n), 256, 0, s>>>(t, p, perm, off, cursor, part, dev_err);
+    if (t.nlos > 0)
+        pair_dr2_kernel<<<t.nlos, 256, 0, s>>>(t, p.pos, p.n, off, part, dr2, dev_err);
 }
 
 void launch_check_emit(const unsigned long long *line_count, const unsigned long long *cursor,

@@ -71,6 +71,7 @@ struct LineGroup {
     int nlines;
     int nc;
     double cw, inv_cw;
+    float cw_f, inv_cw_f;    // float copies for the cell-range superset
     const int *cell_start;   // nc*nc + 1
     const int *cell_line;    // global line ids, grouped by cell
 };
@@ -80,24 +81,45 @@ struct LineTables {
     const double *key;       // index_table.cpp:12-14: cofm[3i+1] (axis 1) or cofm[3i] (axes 2, 3)
     const double *second;    // index_table.cpp:33-39: cofm[3i+1] (axis 3) or cofm[3i+2]
     const int *axis;         // 1-based
-    const float4 *pack;      // per line {key, second, axis bits, 0} in float (prefilter)
+    const float4 *pack;      // per line {key, second, axis bits, inside} in float (prefilter)
     int nlos;
     int n_main;              // lines with axis != 1 (the reference's index_table)
     int n_xx;                // lines with axis == 1 (the reference's index_table_xx)
     double box;
     float box_f;
+    float box_up;            // smallest float f with (double)f > box
     float pre_eps;           // absolute slack of the float prefilter (4 ulp of the box)
 };
 
-// Float copy of the sightline tables for the search prefilter.
-inline float4 pack_line(double key, double second, int axis)
+// Float copy of the sightline tables for the search prefilter.  w = 1 when
+// both coordinates lie in [0, box]: their float copies are then within half
+// an ulp of the box of the double values, which the float accept test uses.
+// Boxes outside [1e-12, 1e18] keep w = 0, so that the float squares of that
+// test neither underflow nor overflow.
+inline float4 pack_line(double key, double second, int axis, double box)
 {
     float4 v;
     v.x = (float)key;
     v.y = (float)second;
     v.z = __int_as_float_host(axis);
-    v.w = 0.f;
+    const bool inside = key >= 0.0 && key <= box && second >= 0.0 && second <= box;
+    v.w = (inside && box >= 1e-12 && box <= 1e18) ? 1.f : 0.f;
     return v;
+}
+
+// The float constants of the tables derived from the box and the cell width.
+inline void set_float_box(LineTables &t, double box)
+{
+    t.box_f = (float)box;
+    float up = t.box_f;
+    if (!((double)up > box))
+        up = __builtin_nextafterf(up, __builtin_inff());
+    t.box_up = up;
+    t.pre_eps = prefilter_eps(box);
+    for (LineGroup &G : t.g) {
+        G.cw_f = (float)G.cw;
+        G.inv_cw_f = (float)G.inv_cw;
+    }
 }
 
 struct Particles {
@@ -134,6 +156,8 @@ struct PairLists {
 // perm (may be null = identity): the order in which particles are visited.
 void launch_count_pairs(const LineTables &t, const Particles &p, const int *perm,
                         unsigned long long *line_count, unsigned char *part_flag, cudaStream_t s);
+// The emit pass writes part[]; dr2[] of every pair follows from it in a
+// second, pair-parallel kernel inside the same launcher.
 void launch_emit_pairs(const LineTables &t, const Particles &p, const int *perm,
                        const long long *off, unsigned long long *cursor, int *part, double *dr2,
                        unsigned *dev_err, cudaStream_t s);

@@ -178,7 +178,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
         const int a = axis[i];
         h_key[i] = (a == 1) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i];
         h_second[i] = (a == 3) ? cofm[3 * (size_t)i + 1] : cofm[3 * (size_t)i + 2];
-        h_pack[i] = pack_line(h_key[i], h_second[i], a);
+        h_pack[i] = pack_line(h_key[i], h_second[i], a, box);
         h_group[a - 1][ng[a - 1]++] = i;
     }
     t.n_xx = ng[0];
@@ -257,8 +257,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     t.second = d_second;
     t.axis = d_axis;
     t.pack = d_pack;
-    t.box_f = (float)box;
-    t.pre_eps = prefilter_eps(box);
+    set_float_box(t, box);
 
     // ---- pair search: count, prefix sum, emit
     Particles p{pos, compute_tau ? vel : nullptr, dens, compute_tau ? temp : nullptr, h,
