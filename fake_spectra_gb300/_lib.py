@@ -56,7 +56,7 @@ _c_size = ctypes.c_size_t
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", _c_int), ("threads", _c_int), ("persistent", _c_int),
-                ("count_work", _c_int), ("reserved", _c_int * 4)]
+                ("count_work", _c_int), ("no_far_tiles", _c_int), ("reserved", _c_int * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -163,9 +163,10 @@ def errbuf():
     return ctypes.create_string_buffer(512)
 
 
-def make_options(precision="fp64", threads=0, persistent=-1, count_work=False):
+def make_options(precision="fp64", threads=0, persistent=-1, count_work=False, far_tiles=True):
     o = Options()
     o.count_work = int(bool(count_work))
+    o.no_far_tiles = int(not far_tiles)
     if precision in ("fp64", FSG_PREC_FP64):
         o.precision = FSG_PREC_FP64
     elif precision in ("fp32", FSG_PREC_FP32):

@@ -285,7 +285,7 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     if (total > 0) {
         launch_emit_pairs(c->tables, p, perm, off, cur, part, dr2, err, s);
         launch_check_emit(cnt, cur, nlos, err, s);
-        c->stats.gpu_launches += 2;
+        c->stats.gpu_launches += 3;   // emit, pair dr2, check
         cuda_check(cudaGetLastError(), "emit_pairs launch");
     }
     // sightline work order: descending pair count (largest first)
@@ -421,9 +421,8 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
     cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int), s), "memset");
     cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
-    launch_deposit(lp, c->tables, p, pl, (const int *)c->line_order.p, nlos, out, ticket, bad,
-                   nbad, err, gacc, ctr, cfg, s);
-    c->stats.gpu_launches++;
+    c->stats.gpu_launches += launch_deposit(lp, c->tables, p, pl, (const int *)c->line_order.p,
+                                            nlos, out, ticket, bad, nbad, err, gacc, ctr, cfg, s);
     cuda_check(cudaGetLastError(), "deposit launch");
     int h_nbad = 0;
     unsigned h_err = 0;
@@ -496,6 +495,7 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
     cfg.threads = (opt && opt->threads > 0 && !vor) ? opt->threads : tmax;
     if (cfg.threads % 32 || cfg.threads > tmax)
         fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
+    cfg.tiles = !(opt && opt->no_far_tiles);
     deposit_plan(cfg, lp.compute_tau, lp.nbins);
     cfg.persistent = (opt && opt->persistent >= 0 && !vor)
                          ? opt->persistent : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
@@ -593,7 +593,8 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
     }
     cuda_check(cudaEventRecord(c->ev[2], s), "event");
     cuda_check(cudaGraphLaunch(c->graph, s), "graph launch");
-    c->stats.gpu_launches += 2 * (int64_t)lps.size();
+    for (const DepositLaunch &cf : cfgs)   // deposit, fallback (+ tile weights)
+        c->stats.gpu_launches += 2 + (nlos > 0 && cf.tiles ? 1 : 0);
     cuda_check(cudaEventRecord(c->ev[3], s), "event");
     unsigned h_err = 0;
     cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");

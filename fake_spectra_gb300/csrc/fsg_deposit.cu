@@ -490,11 +490,12 @@ __host__ __device__ constexpr float binom_f(int n, int k)
 // the warp then walks the staged pairs one after another.
 constexpr int STAGE_CAREFUL = 1 << 30;   // walk in FP64 (see below)
 constexpr int STAGE_SKIP = 1 << 29;      // no overlap (hh^2 <= dr2) or no pair
-constexpr int STAGE_NP = (1 << 29) - 1;  // sub-sample count bits
+constexpr int STAGE_TILES = 1 << 28;     // far wing may be deposited per tile (see below)
+constexpr int STAGE_NP = (1 << 28) - 1;  // sub-sample count bits
 
 struct __align__(16) Stage32 {
     int j0;                  // bin of pixel zmax = floor(v_particle / pixel width)
-    int flags;               // npoints | STAGE_CAREFUL | STAGE_SKIP
+    int flags;               // npoints | STAGE_CAREFUL | STAGE_SKIP | STAGE_TILES
     float base0;             // velocity of pixel zmax's low edge - v_particle
     float inv_b;             // 1 / b
     float scale;             // amp dens / velfac x node spacing / (npoints - 1)
@@ -588,7 +589,14 @@ __device__ __forceinline__ bool stage32_setup(const LineParams &lp, const PairIn
     if (scale_nod)
         *scale_nod = (float)sc;
     st.scale = (float)(sc * (double)in.dens);
-    st.flags = npoints | (careful ? STAGE_CAREFUL : 0);
+    // Far-field tiles need a far wing that decreases with |V|: a positive
+    // scale and non-negative multipole coefficients (the sum is then
+    // increasing in 1/V^2).
+    bool mono = !careful && st.scale > 0.f && isfinite(st.scale);
+#pragma unroll
+    for (int r = 0; r < MP_R; r++)
+        mono = mono && st.A[r] >= 0.f && isfinite(st.A[r]);
+    st.flags = npoints | (careful ? STAGE_CAREFUL : 0) | (mono ? STAGE_TILES : 0);
     return true;
 }
 
@@ -604,6 +612,7 @@ struct Tau32 {
     int j0;
     int npoints;                 // 1: midpoint; else trapezoid points (uniform per pair)
     bool careful;                // walk in FP64 instead (Stage32 flags)
+    bool tiles;                  // far wing may be deposited per tile (Stage32 flags)
 
     __device__ __forceinline__ void load(const Stage32 &st, float bintov_f)
     {
@@ -632,6 +641,7 @@ struct Tau32 {
         vmid0 = v0 + hbin_b;
         npoints = st.flags & STAGE_NP;
         careful = (st.flags & STAGE_CAREFUL) != 0;
+        tiles = (st.flags & STAGE_TILES) != 0 && vk > 0.f;
         sub_dv = npoints > 1 ? __fdividef(bintov, (float)(npoints - 1)) * inv_b : 0.f;
     }
 
@@ -710,12 +720,29 @@ struct Tau32 {
     {
         if (npoints == 1)
             return inner<COUNT>(fmaf(kf, vk, vmid0), tab, ct);
-        const float vlow_b = fmaf(kf, vk, v0);   // (v_low - v_particle) / b
+        return trapezoid<COUNT>(fmaf(kf, vk, v0), tab, ct);   // (v_low - v_particle) / b
+    }
+
+    template <bool COUNT>
+    __device__ __forceinline__ float trapezoid(float vlow_b, const float2 *tab,
+                                               Counters &ct) const
+    {
         float total = 0.5f * inner<COUNT>(vlow_b, tab, ct);
         for (int i = 1; i < npoints - 1; ++i)
             total += inner<COUNT>(fmaf((float)i, sub_dv, vlow_b), tab, ct);
         total += 0.5f * inner<COUNT>(vlow_b + 2.f * hbin_b, tab, ct);
         return total;
+    }
+
+    // taulast at the fractional pixel kf_low + pk (kf_low integral, pk in
+    // [0, 63]): a far-field tile node.  The two-step offset keeps the node's
+    // V as accurate as an integral pixel's.
+    __device__ __forceinline__ float node_value(float kf_low, float pk, const float2 *tab) const
+    {
+        Counters ct;
+        if (npoints == 1)
+            return inner<false>(fmaf(pk, vk, fmaf(kf_low, vk, vmid0)), tab, ct);
+        return trapezoid<false>(fmaf(pk, vk, fmaf(kf_low, vk, v0)), tab, ct);
     }
 };
 
@@ -978,6 +1005,7 @@ struct DepositArgs {
     int smem_mode;
     int persistent;
     int chunk;                      // pairs staged per warp (FP32 tau form)
+    int tiles;                      // far-field tile accumulators (FP32 tau form)
 };
 
 // FMT 0: 128-bit fixed point with carries (FP64 form); 1: split (FP32 form).
@@ -1105,6 +1133,187 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
     }
 }
 
+// ------------------------------------------------------ far-field tiles
+// Far in a pair's damping wing (every pixel of a tile beyond the multipole
+// radius and at least TILE_DIST pixels from the line centre) the FP32 form
+// does not deposit pixel by pixel.  The bins are cut into tiles of TILE_W
+// pixels; for a tile that lies wholly inside the pair's window, the pair adds
+// its contribution at TILE_M Chebyshev nodes of the tile to per-tile node
+// accumulators (the same split fixed point as the pixels).  When the sightline
+// is complete each pixel adds the polynomial interpolant of its tile's node
+// sums, which is linear in the node values and so equals the sum over pairs of
+// each pair's interpolant.  The far wing is a polynomial in 1/V^2 (pole at
+// V = 0), so with the tile half-width at most 0.2 of the distance to the pole
+// the interpolation error of 10 Chebyshev nodes is below 1e-7 of the value
+// (1/V^2: 3e-9, 1/V^4: 1e-7 times its share, which is small that far out).
+// The window rule needs no per-pixel test inside such a tile: the far wing
+// decreases with |V| (STAGE_TILES), and its value equals tautail at a radius
+// V_stop found once per pair by Newton's method on the multipole polynomial;
+// a tile whose farthest pixel centre lies within 0.999 V_stop has every pixel
+// above tautail by far more than the FP32 rounding (the wing falls as 1/V^2,
+// so 2e-3 of tautail), and the window continues past it.  The tile holding the
+// stop pixel, a tile cut by the wrap of the bins and the nbins/2 cap are
+// walked pixel by pixel as before.  The (tile, node) items of a run of tiles
+// are spread over the 32 lanes.
+constexpr int TILE_W = 64;
+constexpr int TILE_M = 10;
+constexpr float TILE_DIST = 128.f;
+
+__device__ double g_tile_w[TILE_W * TILE_M];   // [pixel in tile][node] interpolation weights
+__device__ float g_tile_x[TILE_M];             // node positions, pixels from the tile's first
+
+// Node positions x_k = 31.5 (1 + cos((2k+1) pi / 2M)) rounded to float, and
+// the barycentric Lagrange weights of those float positions at the pixels.
+__global__ void tile_weights_kernel()
+{
+    const int t = threadIdx.x;
+    if (t >= TILE_W * TILE_M)
+        return;
+    const int p = t / TILE_M, k = t % TILE_M;
+    const double h = 0.5 * (TILE_W - 1);
+    double x[TILE_M];
+#pragma unroll
+    for (int i = 0; i < TILE_M; i++)
+        x[i] = (double)(float)(h + h * cos((2 * i + 1) * PI_D / (2 * TILE_M)));
+    double num = 0.0, den = 0.0;
+    bool hit = false;
+#pragma unroll
+    for (int i = 0; i < TILE_M; i++) {
+        double lam = 1.0;
+#pragma unroll
+        for (int j = 0; j < TILE_M; j++)
+            if (j != i)
+                lam /= (x[i] - x[j]);
+        const double d = (double)p - x[i];
+        if (d == 0.0) {
+            hit = true;
+            num = (i == k) ? 1.0 : 0.0;
+            break;
+        }
+        den += lam / d;
+        if (i == k)
+            num = lam / d;
+    }
+    g_tile_w[t] = hit ? num : num / den;
+    if (p == 0)
+        g_tile_x[k] = (float)x[k];
+}
+
+// |V| (in units of b) where the far wing equals tautail: the root of
+// h(W) = sum_r A_r W^(r+1) = tautail in W = 1/V^2.  h is increasing and convex
+// for A_r >= 0, so Newton's method from W0 = tautail / A_0 (h(W0) >= tautail)
+// decreases monotonically to the root.  Returns +inf when tautail <= 0 (the
+// window then runs to the cap) and 0 when the wing is identically zero.
+__device__ __forceinline__ float far_stop_radius(const Tau32 &s, float tautail)
+{
+    if (!(tautail > 0.f))
+        return __int_as_float(0x7f800000);
+    if (!(s.A[0] > 0.f))
+        return 0.f;
+    float W = tautail / s.A[0];
+#pragma unroll 1
+    for (int it = 0; it < 4; it++) {
+        float h = s.A[MP_R - 1], d = (float)MP_R * s.A[MP_R - 1];
+#pragma unroll
+        for (int r = MP_R - 2; r >= 0; r--) {
+            h = fmaf(h, W, s.A[r]);
+            d = fmaf(d, W, (float)(r + 1) * s.A[r]);
+        }
+        W -= (h * W - tautail) / d;
+    }
+    return W > 0.f ? rsqrtf(W) : __int_as_float(0x7f800000);
+}
+
+// The FP32 walk of one pair (not the counting variant) with far-field tiles.
+// Pixel steps as in walk_tau; once the walk is far (see above) a step ends at
+// the next tile boundary, and at a boundary the run of sure tiles ahead is
+// deposited through its nodes.
+__device__ __forceinline__ void walk_tau32_tiled(const DepositArgs &a, const Tau32 &s, int S,
+                                                 unsigned long long *lo, unsigned long long *hi,
+                                                 unsigned long long *tlo,
+                                                 unsigned long long *thi, int *bad, int lane,
+                                                 const float2 *tab)
+{
+    const int nbins = a.lp.nbins;
+    const int half = nbins / 2;
+    const float tautail = (float)a.lp.tautail;
+    const int j0 = s.j0;
+    const float lane_f = (float)lane;
+    const float dmin = fmaxf(s.vmp, TILE_DIST * s.vk);
+    float vsure = -1.f;   // 0.999 V_stop, computed when first needed
+    Counters ct;
+    for (int dir = 0; dir < 2; dir++) {
+        bool far = false, tiles = s.tiles;
+        int k = 0;   // pixels done in this direction
+        while (k < half) {
+            const int koff0 = dir == 0 ? k : -1 - k;
+            const float kf0 = (float)koff0;
+            int len = 32;
+            if (tiles) {
+                if (!far) {
+                    // near edge of pixel k: its low edge going up, high edge going down
+                    const float ve = dir == 0 ? fmaf(kf0, s.vk, s.v0) : -fmaf(kf0 + 1.f, s.vk, s.v0);
+                    far = ve >= dmin;
+                }
+                if (far) {
+                    const int jb = bin_from(j0, koff0, nbins);
+                    const int rem = dir == 0 ? (TILE_W - jb % TILE_W) % TILE_W
+                                             : (jb + 1) % TILE_W;
+                    if (rem == 0) {
+                        if (vsure < 0.f)
+                            vsure = 0.999f * far_stop_radius(s, tautail);
+                        // last pixel (pixels done) whose centre is within vsure:
+                        // |V_mid| = k vk + vmid0 going up, (k + 1) vk - vmid0 going down
+                        const float klim = dir == 0 ? (vsure - s.vmid0) / s.vk
+                                                    : (vsure + s.vmid0) / s.vk - 1.f;
+                        int n = 0;
+                        if (klim >= (float)k + (float)(TILE_W - 1))
+                            n = (int)fminf((klim - (float)k + 1.f) / (float)TILE_W, 1e6f);
+                        n = min(n, (half - k) / TILE_W);
+                        n = min(n, dir == 0 ? (nbins - jb) / TILE_W : (jb + 1) / TILE_W);
+                        if (n > 0) {
+                            const int items = n * TILE_M;
+                            for (int base = 0; base < items; base += 32) {
+                                const int it = base + lane < items ? base + lane : 0;
+                                const int t = it / TILE_M, m = it - t * TILE_M;
+                                const int kt = k + TILE_W * t;
+                                const int klow = dir == 0 ? kt : -kt - TILE_W;   // lowest bin's koff
+                                const int q = (dir == 0 ? jb + TILE_W * t
+                                                        : jb - TILE_W * (t + 1) + 1) / TILE_W;
+                                const float v = s.node_value((float)klow, g_tile_x[m], tab);
+                                if (base + lane < items)
+                                    accumulate<float, 1>(a.dev_err, v, q * TILE_M + m, S, tlo,
+                                                         thi, bad);
+                            }
+                            k += TILE_W * n;
+                            continue;
+                        }
+                        // the stop (or the cap, or the wrap of the bins) is in
+                        // this tile; past the wrap the tiles resume
+                        tiles = dir == 0 ? (nbins - jb < TILE_W) : false;
+                    } else {
+                        len = min(32, rem);
+                    }
+                }
+            }
+            const int kk = k + lane;
+            const bool valid = lane < len && kk < half;
+            const float kf = dir == 0 ? kf0 + lane_f : kf0 - lane_f;
+            // every lane evaluates (warp-uniform fast paths vote inside)
+            const float tl = s.template taulast<false>(kf, a.dev_err, tab, ct);
+            const bool stop = valid && (tl < tautail);
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
+            const int last = m ? (__ffs(m) - 1) : 31;
+            if (valid && lane <= last)
+                accumulate<float, 1>(a.dev_err, tl, bin_from(j0, dir == 0 ? kk : -1 - kk, nbins),
+                                     S, lo, hi, bad);
+            if (m)
+                break;
+            k += len;
+        }
+    }
+}
+
 // FP32 tau form: the warps of the CTA take chunks of `chunk` consecutive pairs
 // of the sightline from a shared counter (dynamic balance: pair costs differ by
 // orders of magnitude); each lane sets up one pair of the chunk into the warp's
@@ -1112,7 +1321,8 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
 template <bool COUNT>
 __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, long long e0,
                                                 long long e1, int S, unsigned long long *lo,
-                                                unsigned long long *hi, int *bad,
+                                                unsigned long long *hi, unsigned long long *tlo,
+                                                unsigned long long *thi, int *bad,
                                                 Stage32 *sw, unsigned *s_chunk,
                                                 const float2 *vtab, double bintov_d, int lane,
                                                 Counters &ct)
@@ -1147,7 +1357,10 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
             }
             Tau32 s;
             s.load(st, bintov_f);
-            walk_tau<1, COUNT, 1>(a, s, S, lo, hi, bad, lane, vtab, ct);
+            if (!COUNT && tlo)
+                walk_tau32_tiled(a, s, S, lo, hi, tlo, thi, bad, lane, vtab);
+            else
+                walk_tau<1, COUNT, 1>(a, s, S, lo, hi, bad, lane, vtab, ct);
         }
         __syncwarp();
     }
@@ -1233,8 +1446,16 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         stage_voigt32(vtab);
     const Bound32 bk(a.lp);
     // dynamic shared memory: [accumulators lo, hi (smem_mode)] [pair staging]
+    // [far-field tile nodes lo, hi (tiles)]
     Stage32 *stage = reinterpret_cast<Stage32 *>(smem + (a.smem_mode ? 2 * (size_t)nbins : 0));
     StageCol32 *stage_col = reinterpret_cast<StageCol32 *>(stage);
+    const int ntiles = nbins / TILE_W;
+    const int nnodes = ntiles * TILE_M;
+    unsigned long long *tlo = nullptr, *thi = nullptr;
+    if (TAU && PREC == 1 && !COUNT && a.tiles && a.smem_mode) {
+        tlo = reinterpret_cast<unsigned long long *>(stage + nwarps * a.chunk);
+        thi = tlo + nnodes;
+    }
     const float btk_abs = (float)fabs(boxtokpc);
     const float col_kfac = (float)(kernel_max(a.lp.kernel) * 1.001);
 
@@ -1275,6 +1496,11 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
             lo[j] = 0ull;
             hi[j] = 0ull;
         }
+        if (tlo)
+            for (int j = threadIdx.x; j < nnodes; j += blockDim.x) {
+                tlo[j] = 0ull;
+                thi[j] = 0ull;
+            }
         if (threadIdx.x == 0)
             s_chunk = 0u;
         __syncthreads();
@@ -1282,8 +1508,9 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         // 2. deposit: warp per pair
         if constexpr (TAU && PREC == 1) {
             if (!s_bad && B > 0.0)
-                deposit_pairs32<COUNT>(a, axis, e0, e1, S, lo, hi, &s_bad, stage + warp * a.chunk,
-                                       &s_chunk, vtab, bintov_d, lane, ct);
+                deposit_pairs32<COUNT>(a, axis, e0, e1, S, lo, hi, tlo, thi, &s_bad,
+                                       stage + warp * a.chunk, &s_chunk, vtab, bintov_d, lane,
+                                       ct);
         } else if constexpr (!TAU && PREC == 1) {
             if (!s_bad && B > 0.0)
                 deposit_pairs_col32<COUNT>(a, axis, e0, e1, S, lo, hi, &s_bad,
@@ -1317,8 +1544,29 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
                 a.bad_lines[atomicAdd(a.n_bad, 1)] = line;
         } else if (B > 0.0) {
             double *row = a.out + (size_t)line * nbins;
-            for (int j = threadIdx.x; j < nbins; j += blockDim.x)
-                row[j] = PREC == 0 ? from_fixed(lo[j], hi[j], S) : from_split(lo[j], hi[j], S);
+            if (tlo) {
+                // node sums to double in place, then pixel + its tile's interpolant
+                double *node = reinterpret_cast<double *>(tlo);
+                for (int j = threadIdx.x; j < nnodes; j += blockDim.x)
+                    node[j] = from_split(tlo[j], thi[j], S);
+                __syncthreads();
+                for (int j = threadIdx.x; j < nbins; j += blockDim.x) {
+                    double v = from_split(lo[j], hi[j], S);
+                    if (j < ntiles * TILE_W) {
+                        const double *w = g_tile_w + (j % TILE_W) * TILE_M;
+                        const double *nd = node + (j / TILE_W) * TILE_M;
+                        double f = 0.0;
+#pragma unroll
+                        for (int m = 0; m < TILE_M; m++)
+                            f = fma(w[m], nd[m], f);
+                        v += f;
+                    }
+                    row[j] = v;
+                }
+            } else {
+                for (int j = threadIdx.x; j < nbins; j += blockDim.x)
+                    row[j] = PREC == 0 ? from_fixed(lo[j], hi[j], S) : from_split(lo[j], hi[j], S);
+            }
         }
         if (!a.persistent)
             break;
@@ -1942,7 +2190,8 @@ size_t stage_pair_bytes(int compute_tau, int precision)
 size_t deposit_smem_bytes(const DepositLaunch &cfg, int compute_tau, int nbins)
 {
     return (cfg.smem_mode ? (size_t)16 * nbins : 0) +
-           (size_t)(cfg.threads / 32) * cfg.chunk * stage_pair_bytes(compute_tau, cfg.precision);
+           (size_t)(cfg.threads / 32) * cfg.chunk * stage_pair_bytes(compute_tau, cfg.precision) +
+           (cfg.tiles ? (size_t)16 * TILE_M * (nbins / TILE_W) : 0);
 }
 
 void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
@@ -1952,20 +2201,30 @@ void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
         // staged pairs per warp: 8 for tau (finer chunks balance the warps
         // better at the end of a sightline, where pair costs differ most), 32
         // (or 16 to keep the accumulators on chip) for the column density
+        // far-field tiles (tau) when their node accumulators fit beside the
+        // pixel accumulators, unless switched off
         const int first = compute_tau ? 8 : 32;
-        for (int chunk : {first, 16, 8}) {
-            if (chunk > first)
+        const bool want_tiles = compute_tau && cfg.tiles;
+        for (int tiles : {1, 0}) {
+            if (tiles && !want_tiles)
                 continue;
-            cfg.chunk = chunk;
-            cfg.smem_mode = 1;
-            if (deposit_smem_bytes(cfg, compute_tau, nbins) <= cap)
-                return;
+            cfg.tiles = tiles;
+            for (int chunk : {first, 16, 8}) {
+                if (chunk > first)
+                    continue;
+                cfg.chunk = chunk;
+                cfg.smem_mode = 1;
+                if (deposit_smem_bytes(cfg, compute_tau, nbins) <= cap)
+                    return;
+            }
         }
+        cfg.tiles = 0;
         cfg.chunk = first;
         cfg.smem_mode = 0;
         return;
     }
     cfg.chunk = 0;
+    cfg.tiles = 0;
     cfg.smem_mode = (size_t)16 * nbins <= cap;
 }
 
@@ -1986,14 +2245,14 @@ int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins)
                          : resident_ctas<false, 0, false>(threads, smem);
 }
 
-void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
-                    const PairLists &pl, const int *line_order, int nlos, double *out,
-                    unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
-                    unsigned long long *gacc, unsigned long long *counters,
-                    const DepositLaunch &cfg, cudaStream_t s)
+int launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
+                   const PairLists &pl, const int *line_order, int nlos, double *out,
+                   unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
+                   unsigned long long *gacc, unsigned long long *counters,
+                   const DepositLaunch &cfg, cudaStream_t s)
 {
     if (nlos == 0)
-        return;
+        return 0;
     DepositArgs a;
     a.lp = lp;
     a.t = t;
@@ -2011,7 +2270,13 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
     a.smem_mode = cfg.smem_mode;
     a.persistent = cfg.persistent;
     a.chunk = cfg.chunk;
+    a.tiles = cfg.tiles;
     const size_t smem = deposit_smem_bytes(cfg, lp.compute_tau, lp.nbins);
+    int launched = 1;
+    if (cfg.tiles && counters == nullptr) {
+        tile_weights_kernel<<<1, TILE_W * TILE_M, 0, s>>>();
+        launched++;
+    }
     const int grid = cfg.persistent ? cfg.grid : nlos;
     const int threads = cfg.threads;
     const bool count = counters != nullptr;
@@ -2030,6 +2295,7 @@ void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &
             count ? launch_one<false, 1, true>(a, grid, threads, smem, s)
                   : launch_one<false, 1, false>(a, grid, threads, smem, s);
     }
+    return launched;
 }
 
 void launch_deposit_fallback(const LineParams &lp, const LineTables &t, const Particles &p,

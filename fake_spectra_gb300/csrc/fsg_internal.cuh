@@ -238,6 +238,7 @@ struct DepositLaunch {
     int grid;                // persistent grid size (CTAs)
     int smem_mode;           // 1: per-sightline shared-memory accumulators
     int chunk;               // pairs staged per warp (FP32 form), else 0
+    int tiles;               // in: allow far-field tiles (FP32 tau); out: planned
 };
 
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines
@@ -245,11 +246,12 @@ struct DepositLaunch {
 // *n_bad) and left for deposit_fallback.
 // counters (may be null): launches the counting variant, which adds {core-branch
 // evals, wing-branch evals, other evals, pixels, multipole wing evals} into counters[0..4].
-void launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
-                    const PairLists &pl, const int *line_order, int nlos, double *out,
-                    unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
-                    unsigned long long *gacc, unsigned long long *counters,
-                    const DepositLaunch &cfg, cudaStream_t s);
+// Returns the number of kernels launched.
+int launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
+                   const PairLists &pl, const int *line_order, int nlos, double *out,
+                   unsigned *ticket, int *bad_lines, int *n_bad, unsigned *dev_err,
+                   unsigned long long *gacc, unsigned long long *counters,
+                   const DepositLaunch &cfg, cudaStream_t s);
 // Chooses cfg.smem_mode and cfg.chunk (cfg.precision and cfg.threads set):
 // shared-memory accumulators whenever they fit beside the pair staging area.
 void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins);

@@ -302,6 +302,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
         DepositLaunch cfg{};
         cfg.precision = precision;
         cfg.threads = threads;
+        cfg.tiles = 1;
         deposit_plan(cfg, compute_tau, nbins);   // smem_mode = 1 within max_bins
         cfg.persistent = precision == FSG_PREC_FP32 ? 1 : 0;
         int sms = 0;

@@ -43,8 +43,9 @@ def _bind_stream(ctx):
 def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, atime, lam, gamma,
                                 fosc, amumass, tautail, pos, vel, dens, temp, h, axis, cofm,
                                 out=None, precision="fp64", threads=0, persistent=-1,
-                                count_work=False):
-    """`_Particle_Interpolate` on device tensors; returns `out` (nlos, nbins) float64 on device."""
+                                count_work=False, far_tiles=True):
+    """`_Particle_Interpolate` on device tensors; returns `out` (nlos, nbins) float64 on device.
+    far_tiles=False deposits the far damping wing of the FP32 form pixel by pixel."""
     import torch
     axis, cofm = _host_tables(axis, cofm)
     nlos = int(axis.shape[0])
@@ -57,7 +58,7 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
               _dptr(temp, "float32", "temp") if compute_tau else None,
               _dptr(h, "float32", "h")]
     _bind_stream(ctx)
-    opt = _lib.make_options(precision, threads, persistent, count_work)
+    opt = _lib.make_options(precision, threads, persistent, count_work, far_tiles)
     eb = _lib.errbuf()
     L = _lib.load()
     rc = L.fsg_particle_interpolate_device(

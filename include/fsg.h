@@ -46,7 +46,10 @@ typedef struct {
     int count_work; /* 1 = run the counting variant of the deposit and report
                        the algorithmic work in fsg_stats (slower; for the
                        roofline only)                                         */
-    int reserved[4];
+    int no_far_tiles; /* FP32 tau: 1 = deposit the far damping wing pixel by
+                       pixel; 0 (default) = through per-tile Chebyshev nodes
+                       where the node accumulators fit on chip               */
+    int reserved[3];
 } fsg_options;
 
 typedef struct {

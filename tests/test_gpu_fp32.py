@@ -137,3 +137,30 @@ def test_work_count_matches_oracle(ctx, port, precision):
     got = st["evals_core"] + st["evals_wing"] + st["evals_other"]
     assert abs(got - evals) <= 1e-3 * evals, (got, evals)
     assert st["pixels"] > 0
+
+
+def test_far_tiles_against_pixel_walk(ctx):
+    # Clump-centred sightlines of 11152-pixel spectra: long damping wings, so
+    # the far-field tiles carry most of the wing.  Tiles on and off (the FP32
+    # pixel-by-pixel wing) both meet the FP32 tolerances against the FP64 form,
+    # and agree with each other to the interpolation accuracy.
+    import torch
+    from fake_spectra_gb300 import interp as I
+    w = synth.config3(nside=64, nlos=96)
+    args = w.call_args(synth.LYA, 1)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in args[11:16]]
+
+    def run(**kw):
+        out = I.particle_interpolate_device(ctx, *args[:11], *dev, args[16], args[17], **kw)
+        return out.cpu().numpy()
+
+    want = run(precision="fp64")
+    on = run(precision="fp32")
+    off = run(precision="fp32", far_tiles=False)
+    assert not np.array_equal(on, off), "no far-field tile was used"
+    check_tau(on, want)
+    check_tau(off, want)
+    sig = off >= 1e-6
+    rel = np.abs(on[sig] - off[sig]) / off[sig]
+    assert rel.max() <= 1e-5, "tiles vs pixel walk: max rel %.3e" % rel.max()
+    assert np.array_equal(on.view(np.int64), run(precision="fp32").view(np.int64))
