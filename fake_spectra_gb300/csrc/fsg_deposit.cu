@@ -727,23 +727,34 @@ struct Tau32 {
     __device__ __forceinline__ float trapezoid(float vlow_b, const float2 *tab,
                                                Counters &ct) const
     {
-        float total = 0.5f * inner<COUNT>(vlow_b, tab, ct);
-        for (int i = 1; i < npoints - 1; ++i)
-            total += inner<COUNT>(fmaf((float)i, sub_dv, vlow_b), tab, ct);
-        total += 0.5f * inner<COUNT>(vlow_b + 2.f * hbin_b, tab, ct);
+        float total = 0.f;
+        for (int i = 0; i < npoints; ++i) {
+            const float x = i == npoints - 1 ? vlow_b + 2.f * hbin_b : fmaf((float)i, sub_dv, vlow_b);
+            const float f = inner<COUNT>(x, tab, ct);
+            total = (i == 0 || i == npoints - 1) ? fmaf(0.5f, f, total) : total + f;
+        }
         return total;
     }
 
-    // taulast at the fractional pixel kf_low + pk (kf_low integral, pk in
-    // [0, 63]): a far-field tile node.  The two-step offset keeps the node's
-    // V as accurate as an integral pixel's.
-    __device__ __forceinline__ float node_value(float kf_low, float pk, const float2 *tab) const
+    // taulast at pixel ka + kb (ka integral; kb = 0 for a pixel, the node's
+    // offset for a far-field tile node).  The two-step offset keeps a node's V
+    // as accurate as an integral pixel's; with kb = 0 the result is taulast's
+    // bit for bit.  One inner() call site keeps the kernel's code small.
+    __device__ __forceinline__ float value_at(float ka, float kb, const float2 *tab) const
     {
         Counters ct;
-        if (npoints == 1)
-            return inner<false>(fmaf(pk, vk, fmaf(kf_low, vk, vmid0)), tab, ct);
-        return trapezoid<false>(fmaf(pk, vk, fmaf(kf_low, vk, v0)), tab, ct);
+        const float x0 = npoints == 1 ? vmid0 : v0;
+        const float x = fmaf(kb, vk, fmaf(ka, vk, x0));
+        float total = 0.f;
+        const int np = npoints;
+        for (int i = 0; i < np; ++i) {
+            const float xi = np == 1 ? x : (i == np - 1 ? x + 2.f * hbin_b : fmaf((float)i, sub_dv, x));
+            const float f = inner<false>(xi, tab, ct);
+            total = (np == 1) ? f : ((i == 0 || i == np - 1) ? fmaf(0.5f, f, total) : total + f);
+        }
+        return total;
     }
+
 };
 
 // Float constants of tau_pair_bound32 (computed once per thread).
@@ -1224,10 +1235,12 @@ __device__ __forceinline__ float far_stop_radius(const Tau32 &s, float tautail)
     return W > 0.f ? rsqrtf(W) : __int_as_float(0x7f800000);
 }
 
-// The FP32 walk of one pair (not the counting variant) with far-field tiles.
-// Pixel steps as in walk_tau; once the walk is far (see above) a step ends at
-// the next tile boundary, and at a boundary the run of sure tiles ahead is
-// deposited through its nodes.
+// The FP32 walk of one pair (not the counting variant; with tlo null, or a
+// pair without STAGE_TILES, it is walk_tau's pixel walk).  Pixel steps as in
+// walk_tau; once the walk is far (see above) a step ends at the next tile
+// boundary, and at a boundary the run of sure tiles ahead is deposited through
+// its nodes, 32 (tile, node) items per round.  Pixel steps and node rounds
+// share one evaluation per lane per iteration.
 __device__ __forceinline__ void walk_tau32_tiled(const DepositArgs &a, const Tau32 &s, int S,
                                                  unsigned long long *lo, unsigned long long *hi,
                                                  unsigned long long *tlo,
@@ -1240,18 +1253,17 @@ __device__ __forceinline__ void walk_tau32_tiled(const DepositArgs &a, const Tau
     const int j0 = s.j0;
     const float lane_f = (float)lane;
     const float dmin = fmaxf(s.vmp, TILE_DIST * s.vk);
-    float vsure = -1.f;   // 0.999 V_stop, computed when first needed
-    Counters ct;
+    float vsure = -1.f;
     for (int dir = 0; dir < 2; dir++) {
-        bool far = false, tiles = s.tiles;
-        int k = 0;   // pixels done in this direction
+        bool far = false, tiles = s.tiles && tlo != nullptr;
+        int k = 0;
+        int n = 0, items = 0, base = 0, jb_run = 0;   // node run state
         while (k < half) {
             const int koff0 = dir == 0 ? k : -1 - k;
             const float kf0 = (float)koff0;
             int len = 32;
-            if (tiles) {
+            if (items == 0 && tiles) {
                 if (!far) {
-                    // near edge of pixel k: its low edge going up, high edge going down
                     const float ve = dir == 0 ? fmaf(kf0, s.vk, s.v0) : -fmaf(kf0 + 1.f, s.vk, s.v0);
                     far = ve >= dmin;
                 }
@@ -1262,52 +1274,63 @@ __device__ __forceinline__ void walk_tau32_tiled(const DepositArgs &a, const Tau
                     if (rem == 0) {
                         if (vsure < 0.f)
                             vsure = 0.999f * far_stop_radius(s, tautail);
-                        // last pixel (pixels done) whose centre is within vsure:
-                        // |V_mid| = k vk + vmid0 going up, (k + 1) vk - vmid0 going down
                         const float klim = dir == 0 ? (vsure - s.vmid0) / s.vk
                                                     : (vsure + s.vmid0) / s.vk - 1.f;
-                        int n = 0;
+                        n = 0;
                         if (klim >= (float)k + (float)(TILE_W - 1))
                             n = (int)fminf((klim - (float)k + 1.f) / (float)TILE_W, 1e6f);
                         n = min(n, (half - k) / TILE_W);
                         n = min(n, dir == 0 ? (nbins - jb) / TILE_W : (jb + 1) / TILE_W);
                         if (n > 0) {
-                            const int items = n * TILE_M;
-                            for (int base = 0; base < items; base += 32) {
-                                const int it = base + lane < items ? base + lane : 0;
-                                const int t = it / TILE_M, m = it - t * TILE_M;
-                                const int kt = k + TILE_W * t;
-                                const int klow = dir == 0 ? kt : -kt - TILE_W;   // lowest bin's koff
-                                const int q = (dir == 0 ? jb + TILE_W * t
-                                                        : jb - TILE_W * (t + 1) + 1) / TILE_W;
-                                const float v = s.node_value((float)klow, g_tile_x[m], tab);
-                                if (base + lane < items)
-                                    accumulate<float, 1>(a.dev_err, v, q * TILE_M + m, S, tlo,
-                                                         thi, bad);
-                            }
-                            k += TILE_W * n;
-                            continue;
+                            items = n * TILE_M;
+                            base = 0;
+                            jb_run = jb;
+                        } else {
+                            tiles = dir == 0 ? (nbins - jb < TILE_W) : false;
                         }
-                        // the stop (or the cap, or the wrap of the bins) is in
-                        // this tile; past the wrap the tiles resume
-                        tiles = dir == 0 ? (nbins - jb < TILE_W) : false;
                     } else {
                         len = min(32, rem);
                     }
                 }
             }
+            // one evaluation per lane: a tile node (node rounds) or a pixel
+            float ka, kb;
+            int idx = 0;
+            bool on = false;
+            if (items) {
+                const int it0 = base + lane;
+                on = it0 < items;
+                const int it = on ? it0 : 0;
+                const int t = it / TILE_M, m = it - t * TILE_M;
+                const int kt = k + TILE_W * t;
+                ka = (float)(dir == 0 ? kt : -kt - TILE_W);
+                kb = g_tile_x[m];
+                idx = (dir == 0 ? jb_run + TILE_W * t : jb_run - TILE_W * (t + 1) + 1) / TILE_W *
+                          TILE_M + m;
+            } else {
+                ka = dir == 0 ? kf0 + lane_f : kf0 - lane_f;
+                kb = 0.f;
+            }
+            const float v = s.value_at(ka, kb, tab);
+            if (items) {
+                if (on)
+                    accumulate<float, 1>(a.dev_err, v, idx, S, tlo, thi, bad);
+                base += 32;
+                if (base >= items) {
+                    k += TILE_W * n;
+                    items = 0;
+                }
+                continue;
+            }
             const int kk = k + lane;
             const bool valid = lane < len && kk < half;
-            const float kf = dir == 0 ? kf0 + lane_f : kf0 - lane_f;
-            // every lane evaluates (warp-uniform fast paths vote inside)
-            const float tl = s.template taulast<false>(kf, a.dev_err, tab, ct);
-            const bool stop = valid && (tl < tautail);
-            const unsigned m = __ballot_sync(0xffffffffu, stop);
-            const int last = m ? (__ffs(m) - 1) : 31;
+            const bool stop = valid && (v < tautail);
+            const unsigned msk = __ballot_sync(0xffffffffu, stop);
+            const int last = msk ? (__ffs(msk) - 1) : 31;
             if (valid && lane <= last)
-                accumulate<float, 1>(a.dev_err, tl, bin_from(j0, dir == 0 ? kk : -1 - kk, nbins),
+                accumulate<float, 1>(a.dev_err, v, bin_from(j0, dir == 0 ? kk : -1 - kk, nbins),
                                      S, lo, hi, bad);
-            if (m)
+            if (msk)
                 break;
             k += len;
         }
@@ -1357,7 +1380,7 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
             }
             Tau32 s;
             s.load(st, bintov_f);
-            if (!COUNT && tlo)
+            if constexpr (!COUNT)
                 walk_tau32_tiled(a, s, S, lo, hi, tlo, thi, bad, lane, vtab);
             else
                 walk_tau<1, COUNT, 1>(a, s, S, lo, hi, bad, lane, vtab, ct);
