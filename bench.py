@@ -50,13 +50,13 @@ F_EVAL = 32
 # evaluations summed by the far-wing multipole form cost 20 flops per pixel
 # (7 evaluations): 20/7 each.
 FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
-# DRAM traffic of the FP32 deposit from one ncu capture of the 192^3 slice of
-# the 256^3 workload (dram__bytes_read.sum + dram__bytes_write.sum, kept with
-# the profile summaries): 3.745 GB read for 7545574 pairs, 0.1905 GB written for
-# 3600 x 6691 pixels; scaled to a launch by pairs (reads) and output pixels
-# (writes).
-TRAFFIC_READ_PER_PAIR = 3.745174e9 / 7545574
-TRAFFIC_WRITE_PER_PIXEL = 0.19050368e9 / (3600 * 6691)
+# DRAM traffic of the FP32 deposit from one ncu capture of the 512^3 workload's
+# recipe at 192^3 particles and 2048 sightlines (dram__bytes_read.sum +
+# dram__bytes_write.sum, kept with the profile summaries): 2.377804 GB read for
+# 5038719 pairs, 0.175254528 GB written for 2048 x 11152 pixels; scaled to a
+# launch by pairs (reads) and output pixels (writes).
+TRAFFIC_READ_PER_PAIR = 2.377804e9 / 5038719
+TRAFFIC_WRITE_PER_PIXEL = 0.175254528e9 / (2048 * 11152)
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
@@ -358,7 +358,8 @@ def main():
                      "peak_fp64": peak64,
                      "traffic": npairs * TRAFFIC_READ_PER_PAIR + pixels * TRAFFIC_WRITE_PER_PIXEL,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
-                                       "192^3 capture, scaled by pairs and output pixels"},
+                                       "192^3 x 2048-sightline capture, scaled by pairs and "
+                                       "output pixels"},
     }
 
     # ---- plain FP64 form on a sightline subset, and the accuracy of FP32 against it
