@@ -678,7 +678,7 @@ struct Tau32 {
         for (int i = 0; i < NODES; ++i) {
             u[i] = U[i] - V;
             wing &= fabsf(u[i]) >= 6.5f;
-            core &= fabsf(u[i]) < 6.0f;
+            core &= fabsf(u[i]) < 11.9f;   // the core form's table ends at 12
         }
         if (__all_sync(0xffffffffu, wing)) {
 #pragma unroll

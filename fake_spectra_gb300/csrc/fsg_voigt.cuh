@@ -142,8 +142,12 @@ __device__ __forceinline__ double voigt_f64(double u, double a)
 //   Im F(x + i a) = a F'(x) - a^3 F'''(x)/6 + a^5 F^(5)(x)/120 - ...
 // (the Taylor series of F in the imaginary direction; the a^7 term is below
 // 1e-7 relative for a <= 0.1).
-//  * x < 6: F and G = F' are read at the nearest x_j = j/10 from a 61-entry
-//    table staged in shared memory; the higher derivatives follow from the
+//  * x < 6 (per node), x < 11.9 (a whole warp step in the core form): F and
+//    G = F' are read at the nearest x_j = j/10 from a 121-entry table staged
+//    in shared memory (the form keeps its accuracy out to x = 12: 5e-7
+//    relative on [6, 12) in an emulation of these float operations against
+//    scipy's wofz, so a warp step whose nodes straddle x = 6 stays in it
+//    instead of running both forms); the higher derivatives follow from the
 //    ODE F' = 1 - 2xF, i.e. F^(n+1) = -2x F^(n) - 2n F^(n-1), and G(x),
 //    F'''(x), F^(5)(x) are Taylor series in d = x - x_j (|d| <= 0.05).
 //  * x >= 6: the asymptotic series of w (A&S 7.1.23) expanded to order a^3:
@@ -153,7 +157,7 @@ __device__ __forceinline__ double voigt_f64(double u, double a)
 // Accuracy ~1e-6 relative against mpmath over a in [0, 0.1]; the residual is
 // the float32 rounding of the argument (relative error of exp(-x^2) ~ 2 x^2 eps).
 // ---------------------------------------------------------------------------
-#define FSG_V32_N 61
+#define FSG_V32_N 121
 
 struct Voigt32 {
     float a, a2, c3, c5, two_a_sqpi, a_sqpi;
@@ -201,7 +205,7 @@ __device__ __forceinline__ float voigt_wing32(float u, const Voigt32 &c)
     return c.a_sqpi * t * fmaf(-c.a2 * t, q, p);
 }
 
-// Core form, valid for |u| < 6.
+// Core form, valid for |u| < 12 (table to x = 12.0).
 // Nearest table index of x >= 0 (x < 6) without int<->float conversions, which
 // run on the narrow FP64/conversion pipe of this GPU: adding 1.5 * 2^23 rounds
 // x*10 to an integer held in the low mantissa bits.

@@ -1,6 +1,6 @@
 """Generate voigt_table.h: real-axis values of the Faddeeva function w(x).
 
-For x_j = j * 0.1 (j = 0 .. 80) the table holds, to full double precision,
+For x_j = j * 0.1 (j = 0 .. 120) the table holds, to full double precision,
   E_j = exp(-x_j^2),
   D_j = (2/sqrt(pi)) F(x_j),            F = Dawson's integral,
   G_j = (2/sqrt(pi)) (1 - 2 x_j F(x_j)) = (2/sqrt(pi)) F'(x_j),
@@ -15,7 +15,7 @@ import mpmath as mp
 
 mp.mp.dps = 60
 H = mp.mpf(1) / 10
-N = 81
+N = 121
 
 
 def dawson(x):
