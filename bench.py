@@ -53,11 +53,11 @@ F_EVAL = 32
 FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 # DRAM traffic of the FP32 deposit from one ncu capture of the 512^3 workload's
 # recipe at 192^3 particles and 2048 sightlines (dram__bytes_read.sum +
-# dram__bytes_write.sum, kept with the profile summaries): 2.377804 GB read for
-# 5038719 pairs, 0.175254528 GB written for 2048 x 11152 pixels; scaled to a
+# dram__bytes_write.sum, kept with the profile summaries): 2.372797 GB read for
+# 5038719 pairs, 0.174416896 GB written for 2048 x 11152 pixels; scaled to a
 # launch by pairs (reads) and output pixels (writes).
-TRAFFIC_READ_PER_PAIR = 2.377804e9 / 5038719
-TRAFFIC_WRITE_PER_PIXEL = 0.175254528e9 / (2048 * 11152)
+TRAFFIC_READ_PER_PAIR = 2.372797e9 / 5038719
+TRAFFIC_WRITE_PER_PIXEL = 0.174416896e9 / (2048 * 11152)
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
@@ -363,6 +363,61 @@ def main():
                                        "output pixels"},
     }
 
+    # ---- end to end through the host-pointer C ABI (copies inside the timed region),
+    # right after the device-resident measurement, under the same conditions
+    if not args.no_e2e:
+        import ctypes
+        from fake_spectra_gb300._spectra_priv import _Particle_Interpolate, _ptr
+        pin = lambda t: t.cpu().pin_memory().numpy()
+        h = [pin(x) for x in (w.pos, w.vel, w.dens["HI"], w.temp, w.hh)]
+        hargs = list(targs[:11]) + h + [w.axis, w.cofm]
+        ke = max(1, min(args.steps, 3))
+        # (a) the C ABI call a host program makes: its own output array,
+        # allocated once; every call copies the inputs in and the spectra out
+        L = _lib.load()
+        opt = _lib.make_options("fp32")
+        eb = _lib.errbuf()
+        tau_h = np.zeros((w.nlos, w.nbins))
+        axis_h, cofm_h = np.ascontiguousarray(w.axis), np.ascontiguousarray(w.cofm)
+
+        def c_call():
+            rc = L.fsg_particle_interpolate(
+                1, w.nbins, int(targs[2]), *[float(x) for x in targs[3:11]],
+                *[_ptr(x) for x in h], w.npart, _ptr(axis_h), _ptr(cofm_h), w.nlos, _ptr(tau_h),
+                ctypes.byref(opt), eb, 512)
+            _lib.raise_for(rc, eb.value.decode(errors="replace"))
+
+        c_call()
+        barrier(world)
+        ck = ClockSampler(local).start()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            c_call()
+        dt = allreduce_max((time.perf_counter() - t0) / ke, world)
+        # (b) the Python drop-in: a new zeroed array per call, as the reference
+        # returns, so each call also pays the first touch and the release of
+        # 2.9 GB of host pages
+        _Particle_Interpolate(*hargs, precision="fp32")
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            tau_d = _Particle_Interpolate(*hargs, precision="fp32")
+        dt_d = allreduce_max((time.perf_counter() - t0) / ke, world)
+        e2e_clk = ck.stop()
+        same = bool(np.array_equal(tau_d, tau_h))
+        del tau_d
+        res["e2e"] = {"value": world * pixels / dt, "unit": "pixels/s",
+                      "h2d_bytes_per_step": int(sum(x.nbytes for x in h)),
+                      "d2h_bytes_per_step": int(tau_h.nbytes),
+                      "ms_per_step": dt * 1e3,
+                      "api": "fsg_particle_interpolate (host pointers; inputs pinned, output a "
+                             "pageable array the caller allocated once)",
+                      "dropin": {"value": world * pixels / dt_d, "ms_per_step": dt_d * 1e3,
+                                 "api": "_spectra_priv._Particle_Interpolate (new output "
+                                        "array per call)",
+                                 "same_result": same},
+                      "clocks": e2e_clk}
+
     # ---- plain FP64 form on a sightline subset, and the accuracy of FP32 against it
     if not args.no_fp64:
         lines = subset_lines(w.nlos, args.fp64_lines)
@@ -539,57 +594,6 @@ def main():
                           "loss": "sum (exp(-tau) - F_target)^2, F_target from seed 5",
                           "grads": "dens, temp, v_los (FP32 backward kernel)"}
         del w4, w4t, dens4, temp4, vel4, ftarget
-
-    # ---- end to end through the host-pointer C ABI (copies inside the timed region)
-    if not args.no_e2e:
-        import ctypes
-        from fake_spectra_gb300._spectra_priv import _Particle_Interpolate, _ptr
-        pin = lambda t: t.cpu().pin_memory().numpy()
-        h = [pin(x) for x in (w.pos, w.vel, w.dens["HI"], w.temp, w.hh)]
-        hargs = list(targs[:11]) + h + [w.axis, w.cofm]
-        ke = max(1, min(args.steps, 3))
-        # (a) the C ABI call a host program makes: its own output array,
-        # allocated once; every call copies the inputs in and the spectra out
-        L = _lib.load()
-        opt = _lib.make_options("fp32")
-        eb = _lib.errbuf()
-        tau_h = np.zeros((w.nlos, w.nbins))
-        axis_h, cofm_h = np.ascontiguousarray(w.axis), np.ascontiguousarray(w.cofm)
-
-        def c_call():
-            rc = L.fsg_particle_interpolate(
-                1, w.nbins, int(targs[2]), *[float(x) for x in targs[3:11]],
-                *[_ptr(x) for x in h], w.npart, _ptr(axis_h), _ptr(cofm_h), w.nlos, _ptr(tau_h),
-                ctypes.byref(opt), eb, 512)
-            _lib.raise_for(rc, eb.value.decode(errors="replace"))
-
-        c_call()
-        barrier(world)
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            c_call()
-        dt = allreduce_max((time.perf_counter() - t0) / ke, world)
-        # (b) the Python drop-in: a new zeroed array per call, as the reference
-        # returns, so each call also pays the first touch and the release of
-        # 2.9 GB of host pages
-        _Particle_Interpolate(*hargs, precision="fp32")
-        barrier(world)
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            tau_d = _Particle_Interpolate(*hargs, precision="fp32")
-        dt_d = allreduce_max((time.perf_counter() - t0) / ke, world)
-        same = bool(np.array_equal(tau_d, tau_h))
-        del tau_d
-        res["e2e"] = {"value": world * pixels / dt, "unit": "pixels/s",
-                      "h2d_bytes_per_step": int(sum(x.nbytes for x in h)),
-                      "d2h_bytes_per_step": int(tau_h.nbytes),
-                      "ms_per_step": dt * 1e3,
-                      "api": "fsg_particle_interpolate (host pointers; inputs pinned, output a "
-                             "pageable array the caller allocated once)",
-                      "dropin": {"value": world * pixels / dt_d, "ms_per_step": dt_d * 1e3,
-                                 "api": "_spectra_priv._Particle_Interpolate (new output "
-                                        "array per call)",
-                                 "same_result": same}}
 
     # ---- CPU baseline: the oracle on a bounded sample of the same workload
     if not args.no_cpu and rank == 0 and world == 1:
