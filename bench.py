@@ -323,7 +323,8 @@ def main():
         "metric": HEADLINE_METRIC, "value": value, "unit": "pixels/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded torch generator (clumpy particles, lognormal fields, sightline grid or random sightlines with a quarter through clump centres)",
+        "data": "synthetic: seeded torch generator (clumpy particles, lognormal fields, "
+                "sightline grid or random sightlines with a quarter through clump centres)",
         "config": {"workload": w.name, "particles": w.npart, "sightlines": w.nlos,
                    "nbins": w.nbins, "pairs": npairs, "line": "Ly-a 1215.67 A",
                    "kernel": "cubic spline", "form": "FP32 tuned (persistent sightline queue)",
