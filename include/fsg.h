@@ -62,7 +62,7 @@ typedef struct {
     /* Work of the last deposit when count_work was set: Voigt-profile
      * evaluations by branch and pixel contributions, for the pixels the
      * reference's tautail window rule evaluates (absorption.cpp:250-278). */
-    int64_t evals_core;      /* FP64: Taylor branch; FP32: |u| < 6 branch      */
+    int64_t evals_core;      /* FP64: Taylor branch; FP32: tabulated core form */
     int64_t evals_wing;      /* asymptotic branch                               */
     int64_t evals_other;     /* a == 0, a < 0 or a > 0.1 (FP32: FP64 profile)   */
     int64_t pixels;          /* pixel contributions                             */

@@ -154,3 +154,33 @@ def test_empty_outputs_need_no_device():
     a = _args(nbins=0)
     out = call(a)
     assert out.shape == (2, 0)
+
+
+def test_struct_layouts(tmp_path):
+    """The ctypes mirrors of fsg_options, fsg_stats and fsg_line have the C
+    header's size and field offsets."""
+    import shutil
+    import subprocess
+    from fake_spectra_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"fsg_options": _lib.Options, "fsg_stats": _lib.Stats, "fsg_line": _lib.Line}
+    rename = {"lambda_": "lambda"}
+    src = ['#include <stddef.h>', '#include <stdio.h>', '#include "fsg.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        src.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in cls._fields_:
+            cf = rename.get(f, f)
+            src.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, cf))
+    src.append("return 0; }")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src))
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), "-o", exe, str(c)], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
