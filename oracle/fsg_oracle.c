@@ -173,6 +173,33 @@ static void w_taylor_axis(double x, double y, double *re, double *im)
     *im = si;
 }
 
+/* Levels of the continued fraction for |z|^2 = r2 >= 49.  Its error falls
+ * quickly with |z|: the levels needed for 2e-16 relative accuracy of both
+ * parts (against 240 levels, over the whole quadrant including the real axis)
+ * are 16, 13, 11, 10, 9, 7, 6, 5 at |z| = 8, 10, 12, 15, 20, 30, 50, 100;
+ * each interval below uses its lower edge's count plus two.  Below |z| = 8
+ * the 24 levels of the fixed form are kept. */
+static int cf_levels(double r2)
+{
+    if (r2 < 64.0)
+        return 24;
+    if (r2 < 100.0)
+        return 18;
+    if (r2 < 144.0)
+        return 15;
+    if (r2 < 225.0)
+        return 13;
+    if (r2 < 400.0)
+        return 12;
+    if (r2 < 900.0)
+        return 11;
+    if (r2 < 2500.0)
+        return 9;
+    if (r2 < 10000.0)
+        return 8;
+    return 7;
+}
+
 /* w(x + iy) for y >= 0, x >= 0 */
 static void w_upper(double x, double y, double *re, double *im)
 {
@@ -185,7 +212,7 @@ static void w_upper(double x, double y, double *re, double *im)
     }
     double r2 = x * x + y * y;
     if (r2 >= 49.0) {
-        w_contfrac(x, y, 24, re, im);
+        w_contfrac(x, y, cf_levels(r2), re, im);
         if (y < 1.0 && x < 9.0) {
             /* exp(-z^2), exponentially small near the axis, beyond the reach of the fraction */
             double m = exp(y * y - x * x);

@@ -76,6 +76,20 @@ def test_voigt_vs_scipy(port):
     assert (np.abs(H - ref) / ref).max() < 1e-12
 
 
+def test_voigt_continued_fraction_levels(port):
+    # the continued fraction's level count steps down with |z| (|z| >= 7): just
+    # above each step, over the quadrant and next to the real axis
+    wofz = pytest.importorskip("scipy.special").wofz
+    rng = np.random.default_rng(3)
+    for r in (7.0, 8.0, 10.0, 12.0, 15.0, 20.0, 30.0, 50.0, 100.0, 1e4):
+        th = np.concatenate([rng.uniform(0, np.pi / 2, 200), [1e-9, 1e-4, np.pi / 2 - 1e-9]])
+        rr = r * (1 + 1e-9)
+        u, a = rr * np.cos(th), np.maximum(rr * np.sin(th), 1e-12)
+        H = np.array([port.voigt(x, y) for x, y in zip(u, a)])
+        ref = wofz(u + 1j * a).real
+        assert (np.abs(H - ref) / np.abs(ref)).max() < 1e-13, r
+
+
 def test_oracle_threads_deterministic(port):
     c = golden("config0_slice.npz")
     t = synth.LYA
