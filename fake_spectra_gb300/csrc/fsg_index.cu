@@ -3,19 +3,22 @@
 //
 // One thread per particle enumerates, for every axis group of sightlines, the
 // transverse grid cells that can hold a sightline within its smoothing length
-// (periodic, minimum image, plus a safety margin), and evaluates the
-// reference's own accept predicate on every candidate with the reference's
-// float/double arithmetic, operation by operation, with no FMA contraction
-// (explicit __fadd_rn / __dmul_rn / __dadd_rn):
+// (periodic, minimum image, plus a safety margin), and decides every
+// candidate by the reference's accept predicate:
 //   * the first-coordinate window [ffm, ffp) of index_table.cpp:89-113,
 //     computed in float and compared against the double multimap key, with
 //     the periodic wrap that splits the range in two;
 //   * second_close, index_table.cpp:52-68 (float window, double compare);
 //   * calc_dr2, index_table.cpp:70-87 (double minimum-image distance), and the
 //     accept test dr2 <= hh*hh with hh*hh a float product (index_table.cpp:45).
-// The cell walk is only a superset generator, so the accepted pair set and
-// every dr2 bit equal the reference's.  Degenerate smoothing lengths are
-// resolved exactly (see for_each_pair).
+// Most candidates are decided by float bounds that imply the predicate's
+// answer (see accept()); the rest get the reference's float/double
+// arithmetic operation by operation, with no FMA contraction (explicit
+// __fadd_rn / __dmul_rn / __dadd_rn).  dr2 of every pair is then computed by
+// pair_dr2_kernel with the same calc_dr2.  The cell walk is only a superset
+// generator, so the accepted pair set and every dr2 bit equal the
+// reference's.  Degenerate smoothing lengths are resolved exactly (see
+// for_each_pair).
 //
 // Particles are first ordered by a 3-D spatial cell (counting sort), so that
 // the 32 lanes of a warp are neighbours: they read the same cells and
