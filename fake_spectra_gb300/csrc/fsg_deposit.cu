@@ -18,7 +18,9 @@
 //   FP64 (plain): every quantity in double, as the reference computes it.
 //   FP32 (tuned): profile, kernel and pixel arithmetic in float; double only
 //     for the particle velocity, the bin of the particle (zmax) and the offset
-//     of the first pixel from it, so box-sized coordinates lose nothing.
+//     of the first pixel from it, so box-sized coordinates lose nothing.  Far
+//     in the damping wing it deposits through per-tile Chebyshev nodes instead
+//     of pixel by pixel (see "far-field tiles").
 //
 // Accumulation: every contribution is converted to a 128-bit two's-complement
 // fixed-point integer with a per-sightline scale 2^S, S chosen from an upper
