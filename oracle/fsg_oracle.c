@@ -147,8 +147,9 @@ static void w_taylor_axis(double x, double y, double *re, double *im)
     double cmr = c0r, cmi = c0i, cr = c1r, ci = c1i;
     int small = 0;
     for (int n = 1; n < 80; n++) {
-        double nr = (-2.0 * x * cr - 2.0 * cmr) / (n + 1);
-        double ni = (-2.0 * x * ci - 2.0 * cmi) / (n + 1);
+        const double inv = 1.0 / (n + 1);
+        double nr = (-2.0 * x * cr - 2.0 * cmr) * inv;
+        double ni = (-2.0 * x * ci - 2.0 * cmi) * inv;
         /* multiply (pr + i pi) by iy */
         double t = pr;
         pr = -pi * y;
