@@ -97,8 +97,12 @@ def parse_args():
     p.add_argument("--nlos", type=int, default=0, help="sightlines (0 = the config's)")
     p.add_argument("--fp64-lines", type=int, default=512,
                    help="sightlines timed in the plain FP64 form (0 = all)")
-    p.add_argument("--cpu-lines", type=int, default=16,
-                   help="sightlines in the CPU baseline sample")
+    p.add_argument("--cpu-per-stratum", type=int, default=11,
+                   help="sightlines per stratum in the CPU baseline sample")
+    p.add_argument("--no-config2", action="store_true",
+                   help="skip the per-line 256^3 three-line report against the oracle")
+    p.add_argument("--no-tophat", action="store_true",
+                   help="skip the 256^3 cubic-spline / top-hat section")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
@@ -204,19 +208,92 @@ def subset_lines(nlos, k, seed=12345):
     return np.sort(rng.choice(nlos, size=k, replace=False))
 
 
-def cpu_sample(w_host, lines, threads):
-    """Time the CPU oracle on a subset of sightlines; returns (pixels/s, seconds)."""
-    import oracle
-    port = oracle.port()
-    port.set_threads(threads)
-    from fake_spectra_gb300 import synth
-    args = list(w_host.call_args(synth.LYA, 1))
-    args[16] = w_host.axis[lines]
-    args[17] = w_host.cofm[lines]
-    t0 = time.perf_counter()
-    port.particle_interpolate(*args)
-    dt = time.perf_counter() - t0
-    return len(lines) * w_host.nbins / dt, dt
+# Port/reference speed factor: the C restatement against the reference's own
+# build on the same inputs (32^3 workload, 64 sightlines, 8 threads, x86 host):
+# 1.61 s against 1.33 s.  The reference build cannot run on the GPU machine.
+PORT_OVER_REFERENCE_TIME = 1.61 / 1.33
+
+
+def strata_of(w):
+    """Strata of the CPU sample: sightline axis x placement (through a clump
+    centre or not, where the workload records it)."""
+    cls = w.line_class if w.line_class is not None else np.zeros(w.nlos, np.int8)
+    keys = sorted(set(zip(w.axis.tolist(), cls.tolist())))
+    return {k: np.nonzero((w.axis == k[0]) & (cls == k[1]))[0] for k in keys}
+
+
+def stratified_picks(strata, per_stratum, seed):
+    rng = np.random.default_rng(seed)
+    return {k: np.sort(rng.choice(v, size=min(per_stratum, len(v)), replace=False))
+            for k, v in strata.items()}
+
+
+class CpuEstimate:
+    """Whole-workload CPU time of the oracle from a stratified sightline sample.
+
+    T = T_search(all sightlines) + sum over strata N_s x (mean thread-seconds per
+    sampled sightline of stratum s) / cores: the oracle's deposit is an OpenMP
+    loop over sightlines (part_int.cpp:25-27), so with N >> cores the threads
+    stay busy and the wall time is the thread time over the cores."""
+
+    def __init__(self, w, strata, cores):
+        self.w, self.strata, self.cores = w, strata, cores
+        self.sec = {k: [] for k in strata}
+        self.t_search_full = None
+        self.npairs_full = None
+
+    def add(self, keys, line_sec):
+        for k, t in zip(keys, line_sec):
+            self.sec[k].append(float(t))
+
+    def seconds(self):
+        dep = sum(len(self.strata[k]) * float(np.mean(v)) / self.cores
+                  for k, v in self.sec.items() if v)
+        return (self.t_search_full or 0.0) + dep, dep
+
+    def value(self):
+        return self.w.nlos * self.w.nbins / self.seconds()[0]
+
+    def describe(self, seed, extra=""):
+        t, dep = self.seconds()
+        per = {"axis%d_%s" % (k[0], "clump" if k[1] else "field"):
+               {"sightlines": int(len(self.strata[k])), "sampled": len(v),
+                "thread_s_per_line": float(np.mean(v)) if v else None}
+               for k, v in self.sec.items()}
+        return {"strata": per, "seed": seed, "search_all_s": self.t_search_full,
+                "deposit_all_s_est": dep, "total_s_est": t,
+                "port_over_reference_time": PORT_OVER_REFERENCE_TIME,
+                "note": "extrapolated: search timed on all %d sightlines; deposit from "
+                        "per-sightline thread seconds of a stratified sample (axis x "
+                        "clump-centred or not), weighted by stratum size, over %d cores. The "
+                        "C restatement runs %.2fx the reference build's time on the same "
+                        "inputs (measured on an x86 host; the reference build cannot run on "
+                        "this machine), so the reference's own CPU rate would be about that "
+                        "factor higher.%s" % (self.w.nlos, self.cores,
+                                             PORT_OVER_REFERENCE_TIME, extra)}
+
+
+def oracle_lines(port, wh, transition, ct, lines, timed=False):
+    """The oracle on the given sightlines (all particles).  timed: also the search
+    seconds and per-sightline thread seconds."""
+    a = list(wh.call_args(transition, ct))
+    a[16], a[17] = wh.axis[lines], wh.cofm[lines]
+    if timed:
+        return port.particle_interpolate_timed(*a)
+    return port.particle_interpolate(*a)
+
+
+def accuracy_stats(got, want, ct):
+    """max|dF|, tau relative error (tau >= 1e-3) or column-density relative error."""
+    if ct:
+        dF = np.abs(np.exp(-got) - np.exp(-want))
+        big = want >= 1e-3
+        rel = np.abs(got - want)[big] / want[big] if big.any() else np.zeros(1)
+        return {"max_abs_dF": float(dF.max()), "tau_rel_err_max": float(rel.max()),
+                "tau_rel_err_median": float(np.median(rel))}
+    nz = want != 0
+    rel = np.abs(got - want)[nz] / np.abs(want[nz]) if nz.any() else np.zeros(1)
+    return {"colden_rel_err_max": float(rel.max())}
 
 
 def run_reference(args):
@@ -224,33 +301,177 @@ def run_reference(args):
     if rank != 0:
         return
     import torch
-    from fake_spectra_gb300 import synth  # noqa: F401
+    import oracle
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     w = make_workload(args, dev).to_host()
     threads = os.cpu_count() or 1
-    lines = subset_lines(w.nlos, args.cpu_lines)
-    for _ in range(args.warmup):
-        cpu_sample(w, lines[:max(1, len(lines) // 4)], threads)
-    vals, secs = [], []
-    for _ in range(args.steps):
-        v, s = cpu_sample(w, lines, threads)
-        vals.append(v)
-        secs.append(s)
-    value = len(lines) * w.nbins * len(secs) / sum(secs)
-    sample = ("CPU oracle (C restatement of the reference path, OpenMP) on %d of %d sightlines "
-              "with all %d particles, per step" % (len(lines), w.nlos, w.npart))
+    port = oracle.port()
+    port.set_threads(threads)
+    strata = strata_of(w)
+    keys = sorted(strata)
+    picks = stratified_picks(strata, args.cpu_per_stratum, seed=12345)
+    est = CpuEstimate(w, strata, threads)
+    est.t_search_full, est.npairs_full = port.search_seconds(w.pos, w.hh, w.axis, w.cofm, w.box)
+    rounds = max(len(v) for v in picks.values())
+
+    def one_round(r):
+        lines = np.array([picks[k][r % len(picks[k])] for k in keys])
+        t0 = time.perf_counter()
+        _, _, sec = oracle_lines(port, w, synth_lya(), 1, lines, timed=True)
+        return time.perf_counter() - t0, sec
+
+    for r in range(args.warmup):
+        one_round(rounds - 1 - r % rounds)
+    walls = []
+    for step in range(args.steps):
+        dt, sec = one_round(step % rounds)
+        walls.append(dt)
+        est.add(keys, sec)
+    value = est.value()
+    sample = ("CPU oracle (C restatement of the reference path, OpenMP, %d threads); each step "
+              "one sightline from each of the %d strata (axis x clump-centred or not) with all "
+              "%d particles" % (threads, len(keys), w.npart))
     print(json.dumps({
         "impl": "reference", "metric": HEADLINE_METRIC, "value": value, "unit": "pixels/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
+        "ms_per_step": 1e3 * sum(walls) / len(walls), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w.name, "particles": w.npart, "sightlines": w.nlos,
                    "nbins": w.nbins, "line": "Ly-a 1215.67 A", "kernel": "cubic spline"},
         "cpu_baseline": {"value": value, "unit": "pixels/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "estimate": est.describe(12345)},
         "e2e": {"value": value, "unit": "pixels/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))
+
+
+def synth_lya():
+    from fake_spectra_gb300 import synth
+    return synth.LYA
+
+
+def config2_report(ctx, interp, synth):
+    """Ly-a, Ly-b and CIV 1548 on the 256^3 three-line workload: the batched FP32
+    call over all 3600 sightlines and FP64 calls on a sightline sample, each
+    against the oracle on that sample (the 6 sightlines with the most pairs and
+    18 random ones), per line, for tau and column density."""
+    import torch
+    import oracle
+    port = oracle.port()
+    port.set_threads(os.cpu_count() or 1)
+    w2 = synth.generate_torch(2, device="cuda")
+    npairs = interp.build_pairs(ctx, w2.box, w2.pos, w2.hh, w2.axis, w2.cofm)
+    off, _, _ = interp.copy_pairs(ctx, w2.nlos, npairs, sorted=False)
+    cnt = np.diff(off)
+    top = np.argsort(-cnt, kind="stable")[:6]
+    rng = np.random.default_rng(2024)
+    lines = np.sort(np.concatenate([top, rng.choice(np.setdiff1d(np.arange(w2.nlos), top),
+                                                    size=18, replace=False)]))
+    wh = w2.to_host()
+    _, ppart, _ = port.near_particles(wh.pos, wh.hh, w2.axis[lines], w2.cofm[lines], w2.box)
+    sub = np.unique(ppart)
+    blines = [(t, w2.dens[t.species], True, True) for t in w2.transitions]
+
+    def batch():
+        return interp.spectra_batch_device(ctx, w2.nbins, w2.kernel, w2.box, w2.velfac,
+                                           w2.atime, w2.tautail, w2.pos, w2.vel, w2.temp, w2.hh,
+                                           w2.axis, w2.cofm, blines, precision="fp32")
+    outs = batch()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    outs = batch()
+    torch.cuda.synchronize()
+    ms_batch = (time.perf_counter() - t0) * 1e3
+    rows = torch.from_numpy(lines).cuda()
+    per_line = {}
+    for (t, _, _, _), (tau_t, col_t) in zip(blines, outs):
+        r = {}
+        for ct, full in ((1, tau_t), (0, col_t)):
+            a = list(w2.call_args(t, ct))
+            a[16], a[17] = w2.axis[lines], w2.cofm[lines]
+            g64 = interp.particle_interpolate_device(ctx, *a, precision="fp64").cpu().numpy()
+            ha = list(wh.call_args(t, ct))
+            for k in range(11, 16):
+                ha[k] = ha[k][sub]
+            ha[16], ha[17] = wh.axis[lines], wh.cofm[lines]
+            want = port.particle_interpolate(*ha)
+            g32 = full[rows].cpu().numpy()
+            for form, got in (("fp32", g32), ("fp64", g64)):
+                r.setdefault(form, {}).update(accuracy_stats(got, want, ct))
+        per_line[t.name] = r
+    del outs
+    return {"workload": w2.name, "particles": w2.npart, "sightlines_total": w2.nlos,
+            "nbins": w2.nbins, "sightlines_compared": int(len(lines)),
+            "sample": "the 6 sightlines with the most pairs and 18 random ones (seed 2024)",
+            "fp32": "one batched call over all sightlines (search + one CUDA graph of 3 tau + "
+                    "3 column-density deposits): %.1f ms" % ms_batch,
+            "fp64": "one call per line and quantity on the sampled sightlines",
+            "against": "CPU oracle (FP64 C restatement, pinned to the reference build)",
+            "lines": per_line}
+
+
+def config1_kernels(ctx, interp, synth, stream, with_cpu=True):
+    """The 256^3 workload (3600 sightlines x 6691 pixels, Ly-a) with the cubic
+    spline and the top-hat kernel: FP32 over all sightlines, FP64 on a 600-line
+    subset, the CPU oracle's estimate for the whole workload from 8 sampled
+    sightlines, and both GPU forms against the oracle on those 8."""
+    import torch
+    w1 = synth.generate_torch(1, device="cuda")
+    lya = synth.LYA
+    wh = w1.to_host() if with_cpu else None
+    sub = subset_lines(w1.nlos, 600, seed=31)
+    samp = subset_lines(w1.nlos, 8, seed=32)
+    pixels = w1.nlos * w1.nbins
+    out = {"workload": w1.name, "particles": w1.npart, "sightlines": w1.nlos,
+           "nbins": w1.nbins}
+    if with_cpu:
+        import oracle
+        port = oracle.port()
+        threads = os.cpu_count() or 1
+        port.set_threads(threads)
+        t_search, _ = port.search_seconds(wh.pos, wh.hh, wh.axis, wh.cofm, wh.box)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for kernel, name in ((1, "cubic_spline"), (0, "top_hat")):
+        a = list(w1.call_args(lya, 1, kernel=kernel))
+        o = torch.empty((w1.nlos, w1.nbins), dtype=torch.float64, device="cuda")
+        interp.particle_interpolate_device(ctx, *a, out=o, precision="fp32")
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            interp.particle_interpolate_device(ctx, *a, out=o, precision="fp32")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1) / 3
+        a64 = list(a)
+        a64[16], a64[17] = w1.axis[sub], w1.cofm[sub]
+        o64 = torch.empty((len(sub), w1.nbins), dtype=torch.float64, device="cuda")
+        e0.record(stream)
+        interp.particle_interpolate_device(ctx, *a64, out=o64, precision="fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        r = {"fp32": {"value": pixels / (ms32 * 1e-3), "unit": "pixels/s", "ms_per_call": ms32,
+                      "sightlines": w1.nlos},
+             "fp64": {"value": len(sub) * w1.nbins / (ms64 * 1e-3), "unit": "pixels/s",
+                      "ms_per_call": ms64, "sightlines": int(len(sub))}}
+        if with_cpu:
+            ha = list(wh.call_args(lya, 1, kernel=kernel))
+            ha[16], ha[17] = wh.axis[samp], wh.cofm[samp]
+            want, _, sec = port.particle_interpolate_timed(*ha)
+            t_all = t_search + w1.nlos * float(np.mean(sec)) / threads
+            r["cpu"] = {"value": pixels / t_all, "unit": "pixels/s", "cores": threads,
+                        "kind": "port", "estimate_s": t_all,
+                        "sample": "search timed on all sightlines (%.1f s); deposit from the "
+                                  "thread seconds of 8 random sightlines" % t_search}
+            g32 = o[torch.from_numpy(samp).cuda()].cpu().numpy()
+            a64[16], a64[17] = w1.axis[samp], w1.cofm[samp]
+            g64 = interp.particle_interpolate_device(ctx, *a64, precision="fp64").cpu().numpy()
+            r["fp32"].update(accuracy_stats(g32, want, 1))
+            r["fp64"].update(accuracy_stats(g64, want, 1))
+            r["compared_sightlines"] = 8
+        out[name] = r
+        del o, o64
+    return out
 
 
 def main():
@@ -596,16 +817,62 @@ def main():
                           "grads": "dens, temp, v_los (FP32 backward kernel)"}
         del w4, w4t, dens4, temp4, vel4, ftarget
 
-    # ---- CPU baseline: the oracle on a bounded sample of the same workload
+    # ---- CPU baseline: the oracle on a stratified sample of the same workload, and
+    # the accuracy of both GPU forms against the oracle's output on those sightlines
     if not args.no_cpu and rank == 0 and world == 1:
+        import oracle
         wh = w.to_host()
         threads = os.cpu_count() or 1
-        lines = subset_lines(w.nlos, args.cpu_lines, seed=777)
-        v, s = cpu_sample(wh, lines, threads)
-        res["cpu_baseline"] = {"value": v, "unit": "pixels/s", "cores": threads, "kind": "port",
-                               "sample": "CPU oracle (C restatement, OpenMP) on %d random of %d "
-                                         "sightlines with all %d particles: %.1f s"
-                                         % (len(lines), w.nlos, w.npart, s)}
+        port = oracle.port()
+        port.set_threads(threads)
+        strata = strata_of(w)
+        keys = sorted(strata)
+        picks = stratified_picks(strata, args.cpu_per_stratum, seed=777)
+        lines = np.concatenate([picks[k] for k in keys])
+        est = CpuEstimate(w, strata, threads)
+        est.t_search_full, est.npairs_full = port.search_seconds(wh.pos, wh.hh, wh.axis,
+                                                                 wh.cofm, wh.box)
+        t0 = time.perf_counter()
+        want, t_s, sec = oracle_lines(port, wh, lya, 1, lines, timed=True)
+        wall = time.perf_counter() - t0
+        est.add([k for k in keys for _ in picks[k]], sec)
+        v = est.value()
+        res["cpu_baseline"] = {
+            "value": v, "unit": "pixels/s", "cores": threads, "kind": "port",
+            "sample": "CPU oracle (C restatement, OpenMP, %d threads) on a stratified sample of "
+                      "%d of %d sightlines (%d per stratum of axis x clump-centred or not, seed "
+                      "777) with all %d particles: %.1f s wall (%.3g px/s on the sample itself); "
+                      "the search over all sightlines %.1f s" % (
+                          threads, len(lines), w.nlos, args.cpu_per_stratum, w.npart, wall,
+                          len(lines) * w.nbins / wall, est.t_search_full),
+            "estimate": est.describe(777)}
+        # accuracy of the GPU forms against the oracle on the sampled sightlines
+        rows = torch.from_numpy(lines).cuda()
+        g32 = tau32[rows].cpu().numpy()
+        o64 = torch.empty((len(lines), w.nbins), dtype=torch.float64, device="cuda")
+        g64 = step("fp64", o=o64, lines=lines).cpu().numpy()
+        want_c = oracle_lines(port, wh, lya, 0, lines)
+        cargs = list(w.call_args(lya, 0))
+        cargs[16], cargs[17] = w.axis[lines], w.cofm[lines]
+        c32 = interp.particle_interpolate_device(ctx, *cargs, precision="fp32").cpu().numpy()
+        c64 = interp.particle_interpolate_device(ctx, *cargs, precision="fp64").cpu().numpy()
+        res.setdefault("accuracy", {})["vs_oracle"] = {
+            "sightlines": int(len(lines)),
+            "sample": "the CPU baseline's stratified sample (seed 777)",
+            "fp32": {**accuracy_stats(g32, want, 1), **accuracy_stats(c32, want_c, 0),
+                     "from": "the timed full-size FP32 call (all sightlines)"},
+            "fp64": {**accuracy_stats(g64, want, 1), **accuracy_stats(c64, want_c, 0),
+                     "from": "an FP64 call on the sampled sightlines"}}
+        del o64, rows
+
+    # ---- 256^3 workload with three lines: per line, both GPU forms against the oracle
+    if not args.no_config2 and not args.no_cpu and rank == 0 and world == 1:
+        res["config2_per_line"] = config2_report(ctx, interp, synth)
+
+    # ---- 256^3 workload (60 x 60 grid along axis 3): cubic spline and top hat
+    if not args.no_tophat and rank == 0 and world == 1:
+        res["config1_kernels"] = config1_kernels(ctx, interp, synth, stream,
+                                                 with_cpu=not args.no_cpu)
     if rank == 0:
         print(json.dumps(res))
 

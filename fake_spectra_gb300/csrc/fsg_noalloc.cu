@@ -14,17 +14,22 @@
 //
 // Limits: at most NOALLOC_MAX_LINES sightlines, as many pairs as fit in the
 // rest of the array (about 5.4 million), and nbins small enough for the
-// per-sightline accumulators to sit in shared memory; larger calls are
-// rejected with FSG_ERR_VALUE and a message naming the limit.
+// per-sightline accumulators to sit in shared memory (the per-form figures
+// are in include/fsg.h); larger calls are rejected with FSG_ERR_VALUE and a
+// message naming the limit.
 //
 // The array's address is looked up with cudaGetSymbolAddress on the first call
 // on each device, with that device current; that first call should therefore
-// come before any stream capture.  All calls share the array and it keeps the
-// previous call's contents (everything that must start at zero is cleared by
-// each call).  Calls are serialised by a process-wide lock and return only after
-// their GPU work has finished; GPU work that overlapped a call using the same
-// array (for example from another thread bypassing this entry point's lock)
-// would race on it.
+// come before any stream capture.  The address is kept for the life of the
+// process, so a cudaDeviceReset between calls is not supported.  The particle
+// arrays and the output must be device memory of the current device (checked
+// with cudaPointerGetAttributes before anything is queued).  All calls share
+// the array and it keeps the previous call's contents (everything that must
+// start at zero is cleared by each call).  Calls are serialised by a
+// process-wide lock and return only after their GPU work has finished, on
+// error paths as well; GPU work that overlapped a call using the same array
+// (for example from another thread bypassing this entry point's lock) would
+// race on it.
 #include "fsg.h"
 #include "fsg_internal.cuh"
 
@@ -115,59 +120,52 @@ LineParams noalloc_line_params(int compute_tau, int nbins, int kernel, double bo
 
 }  // namespace
 
-extern "C" int fsg_particle_interpolate_noalloc(
-    int compute_tau, int nbins, int kernel, double box, double velfac, double atime,
-    double lambda, double gamma, double fosc, double amumass, double tautail, const float *pos,
-    const float *vel, const float *dens, const float *temp, const float *h, int64_t npart,
-    const int32_t *axis, const double *cofm, int32_t nlos, double *out, int precision,
-    void *stream, char *errbuf, size_t errlen)
-{
-    (void)atime;
-    // ---- argument checks (same rules as the allocating entry points, plus the limits)
-    if (nbins < 0 || npart < 0 || nlos < 0)
-        return set_error(errbuf, errlen, FSG_ERR_VALUE, "negative size");
-    if (kernel == VORONOI)
-        return set_error(errbuf, errlen, FSG_ERR_NOT_IMPLEMENTED,
-                         "the Voronoi-mesh kernel (kernel == 2) is not implemented");
-    if (!(box > 0.0) || !std::isfinite(box))
-        return set_error(errbuf, errlen, FSG_ERR_VALUE, "box size must be positive and finite");
-    if (precision != FSG_PREC_FP64 && precision != FSG_PREC_FP32)
-        return set_error(errbuf, errlen, FSG_ERR_VALUE, "unknown precision %d", precision);
-    if (npart > 2147483647LL)
-        return set_error(errbuf, errlen, FSG_ERR_VALUE, "at most 2^31-1 particles");
-    if (nlos > NOALLOC_MAX_LINES)
-        return set_error(errbuf, errlen, FSG_ERR_VALUE,
-                         "%d sightlines exceed the no-allocation limit of %d", nlos,
-                         NOALLOC_MAX_LINES);
-    for (int i = 0; i < nlos; i++) {
-        if (axis[i] < 1 || axis[i] > 3)
-            return set_error(errbuf, errlen, FSG_ERR_VALUE,
-                             "axis[%d] = %d: sightline axes must be 1, 2 or 3", i, axis[i]);
-        for (int k = 0; k < 3; k++)
-            if (!std::isfinite(cofm[3 * (size_t)i + k]))
-                return set_error(errbuf, errlen, FSG_ERR_VALUE, "cofm[%d] is not finite", i);
-    }
-    if (nlos == 0 || nbins == 0)
-        return FSG_OK;
-    const int threads = precision == FSG_PREC_FP64 ? 256 : 512;
-    const int max_bins = deposit_max_smem_bins(compute_tau, precision, threads);
-    if (nbins > max_bins)
-        return set_error(errbuf, errlen, FSG_ERR_VALUE,
-                         "nbins = %d exceeds the no-allocation limit of %d pixels (accumulators "
-                         "must fit in shared memory)", nbins, max_bins);
+namespace {
 
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+// The body of fsg_particle_interpolate_noalloc after its argument checks, run
+// under the lock.  `enqueued` is set once GPU work has been queued on the
+// stream, so that the caller can wait for it on every error return.
+int noalloc_run(int compute_tau, int nbins, int kernel, double box, double velfac,
+                double lambda, double gamma, double fosc, double amumass, double tautail,
+                const float *pos, const float *vel, const float *dens, const float *temp,
+                const float *h, int64_t npart, const int32_t *axis, const double *cofm,
+                int32_t nlos, double *out, int precision, int threads, cudaStream_t stream_in,
+                bool &enqueued, char *errbuf, size_t errlen)
+{
     int dev = 0;
     NA_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return set_error(errbuf, errlen, FSG_ERR_VALUE, "device ordinal %d out of range", dev);
+    // the arrays must be device memory of the current device: the scratch
+    // address, the stream and every launch below belong to that device
+    {
+        const void *ptrs[] = {pos, h, dens, compute_tau ? vel : nullptr,
+                              compute_tau ? temp : nullptr, out};
+        const char *names[] = {"pos", "h", "dens", "vel", "temp", "out"};
+        for (int k = 0; k < 6; k++) {
+            if (!ptrs[k] || (k < 5 && npart == 0))
+                continue;
+            cudaPointerAttributes at{};
+            NA_CUDA(cudaPointerGetAttributes(&at, ptrs[k]), "cudaPointerGetAttributes");
+            if (at.type == cudaMemoryTypeManaged)
+                continue;
+            if (at.type != cudaMemoryTypeDevice)
+                return set_error(errbuf, errlen, FSG_ERR_VALUE,
+                                 "%s is not device memory (this entry point takes device "
+                                 "pointers)", names[k]);
+            if (at.device != dev)
+                return set_error(errbuf, errlen, FSG_ERR_VALUE,
+                                 "%s is on device %d but device %d is current", names[k],
+                                 at.device, dev);
+        }
+    }
     if (!g_noalloc_addr[dev]) {
         // once per device, with that device current
         void *p = nullptr;
         NA_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress");
         g_noalloc_addr[dev] = p;
     }
-    cudaStream_t s = (cudaStream_t)stream;
+    cudaStream_t s = stream_in;
 
     // ---- sightline tables on the host (static staging)
     LineTables t{};
@@ -222,6 +220,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
         int *cl = (int *)cv.take(sizeof(int) * n);
         if (!cl)
             return set_error(errbuf, errlen, FSG_ERR_VALUE, "no-allocation scratch exhausted");
+        enqueued = true;
         NA_CUDA(cudaMemcpyAsync(cs, h_cell_start[g], sizeof(int) * (ncell + 1),
                                 cudaMemcpyHostToDevice, s), "upload cells");
         NA_CUDA(cudaMemcpyAsync(cl, h_cell_line[g], sizeof(int) * n, cudaMemcpyHostToDevice, s),
@@ -245,6 +244,7 @@ extern "C" int fsg_particle_interpolate_noalloc(
     double *d_dr2 = (double *)cv.take(8ull * pair_cap);
     if (!d_dr2)
         return set_error(errbuf, errlen, FSG_ERR_VALUE, "no-allocation scratch exhausted");
+    enqueued = true;
     NA_CUDA(cudaMemcpyAsync(d_key, h_key, sizeof(double) * nlos, cudaMemcpyHostToDevice, s),
             "upload sightlines");
     NA_CUDA(cudaMemcpyAsync(d_second, h_second, sizeof(double) * nlos, cudaMemcpyHostToDevice,
@@ -330,4 +330,59 @@ extern "C" int fsg_particle_interpolate_noalloc(
                          "kernels reported device error bits 0x%x (%s)", h_err,
                          deverr_text(h_err).c_str());
     return FSG_OK;
+}
+
+}  // namespace
+
+extern "C" int fsg_particle_interpolate_noalloc(
+    int compute_tau, int nbins, int kernel, double box, double velfac, double atime,
+    double lambda, double gamma, double fosc, double amumass, double tautail, const float *pos,
+    const float *vel, const float *dens, const float *temp, const float *h, int64_t npart,
+    const int32_t *axis, const double *cofm, int32_t nlos, double *out, int precision,
+    void *stream, char *errbuf, size_t errlen)
+{
+    (void)atime;
+    // ---- argument checks (same rules as the allocating entry points, plus the limits)
+    if (nbins < 0 || npart < 0 || nlos < 0)
+        return set_error(errbuf, errlen, FSG_ERR_VALUE, "negative size");
+    if (kernel == VORONOI)
+        return set_error(errbuf, errlen, FSG_ERR_NOT_IMPLEMENTED,
+                         "the Voronoi-mesh kernel (kernel == 2) is not implemented");
+    if (!(box > 0.0) || !std::isfinite(box))
+        return set_error(errbuf, errlen, FSG_ERR_VALUE, "box size must be positive and finite");
+    if (precision != FSG_PREC_FP64 && precision != FSG_PREC_FP32)
+        return set_error(errbuf, errlen, FSG_ERR_VALUE, "unknown precision %d", precision);
+    if (npart > 2147483647LL)
+        return set_error(errbuf, errlen, FSG_ERR_VALUE, "at most 2^31-1 particles");
+    if (nlos > NOALLOC_MAX_LINES)
+        return set_error(errbuf, errlen, FSG_ERR_VALUE,
+                         "%d sightlines exceed the no-allocation limit of %d", nlos,
+                         NOALLOC_MAX_LINES);
+    for (int i = 0; i < nlos; i++) {
+        if (axis[i] < 1 || axis[i] > 3)
+            return set_error(errbuf, errlen, FSG_ERR_VALUE,
+                             "axis[%d] = %d: sightline axes must be 1, 2 or 3", i, axis[i]);
+        for (int k = 0; k < 3; k++)
+            if (!std::isfinite(cofm[3 * (size_t)i + k]))
+                return set_error(errbuf, errlen, FSG_ERR_VALUE, "cofm[%d] is not finite", i);
+    }
+    if (nlos == 0 || nbins == 0)
+        return FSG_OK;
+    const int threads = precision == FSG_PREC_FP64 ? 256 : 512;
+    const int max_bins = deposit_max_smem_bins(compute_tau, precision, threads);
+    if (nbins > max_bins)
+        return set_error(errbuf, errlen, FSG_ERR_VALUE,
+                         "nbins = %d exceeds the no-allocation limit of %d pixels (accumulators "
+                         "must fit in shared memory)", nbins, max_bins);
+
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    bool enqueued = false;
+    const int rc = noalloc_run(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                               amumass, tautail, pos, vel, dens, temp, h, npart, axis, cofm, nlos,
+                               out, precision, threads, (cudaStream_t)stream, enqueued, errbuf,
+                               errlen);
+    // every return leaves no work of this call in flight on the shared array
+    if (rc != FSG_OK && enqueued)
+        (void)cudaStreamSynchronize((cudaStream_t)stream);
+    return rc;
 }

@@ -222,25 +222,28 @@ def particle_interpolate_noalloc(compute_tau, nbins, kernel, box, velfac, atime,
     For callers that may not call cudaMalloc (their application owns the GPU's
     memory).  Scratch is a fixed 64 MiB array inside the library; limits: at
     most 8192 sightlines, about 5.4 million sightline-particle pairs, and nbins
-    within the shared-memory capacity.  `out` (float64, device) is the only
-    buffer the caller provides; allocate it up front if allocation is not
-    allowed at call time."""
+    within the shared-memory capacity (include/fsg.h gives the figure for each
+    form).  The call runs on the device that holds `pos`.  `out` (float64, on
+    that device) is the only buffer the caller provides; allocate it up front
+    if allocation is not allowed at call time."""
     import torch
     axis, cofm = _host_tables(axis, cofm)
     nlos = int(axis.shape[0])
-    if out is None:
-        out = torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device)
-    prec = _lib.make_options(precision).precision
-    eb = _lib.errbuf()
-    L = _lib.load()
-    rc = L.fsg_particle_interpolate_noalloc(
-        int(compute_tau), int(nbins), int(kernel), float(box), float(velfac), float(atime),
-        float(lam), float(gamma), float(fosc), float(amumass), float(tautail),
-        _dptr(pos, "float32", "pos"), _dptr(vel, "float32", "vel") if compute_tau else None,
-        _dptr(dens, "float32", "dens"), _dptr(temp, "float32", "temp") if compute_tau else None,
-        _dptr(h, "float32", "h"), int(pos.shape[0]), axis.ctypes.data_as(ctypes.c_void_p),
-        cofm.ctypes.data_as(ctypes.c_void_p), nlos, _dptr(out, "float64", "out"), prec,
-        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), eb, 512)
+    # the C side works on the current device: make it the one the data is on
+    with torch.cuda.device(pos.device):
+        if out is None:
+            out = torch.empty((nlos, int(nbins)), dtype=torch.float64, device=pos.device)
+        prec = _lib.make_options(precision).precision
+        eb = _lib.errbuf()
+        L = _lib.load()
+        rc = L.fsg_particle_interpolate_noalloc(
+            int(compute_tau), int(nbins), int(kernel), float(box), float(velfac), float(atime),
+            float(lam), float(gamma), float(fosc), float(amumass), float(tautail),
+            _dptr(pos, "float32", "pos"), _dptr(vel, "float32", "vel") if compute_tau else None,
+            _dptr(dens, "float32", "dens"),
+            _dptr(temp, "float32", "temp") if compute_tau else None,
+            _dptr(h, "float32", "h"), int(pos.shape[0]), axis.ctypes.data_as(ctypes.c_void_p),
+            cofm.ctypes.data_as(ctypes.c_void_p), nlos, _dptr(out, "float64", "out"), prec,
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), eb, 512)
     _lib.raise_for(rc, eb.value.decode(errors="replace"))
     return out
-

@@ -21,7 +21,7 @@ Interpretations made here (stated, not taken from the reference):
 * Clump positions wrap periodically into the box.
 """
 from dataclasses import dataclass, field
-from typing import Dict, List
+from typing import Dict, List, Optional
 
 import numpy as np
 
@@ -73,6 +73,9 @@ class Workload:
     cofm: np.ndarray         # (NumLos, 3) float64
     transitions: List[Transition] = field(default_factory=list)
     tautail: float = 1e-7    # spectra.py:135
+    # per sightline: 1 where it was placed through a clump centre, else 0
+    # (None for workloads without that placement)
+    line_class: Optional[np.ndarray] = None
 
     @property
     def npart(self):
@@ -277,8 +280,10 @@ def config3(seed=3, nside=512, nlos=32768):
     through = rng.random(nlos) < 0.25
     pick = rng.integers(0, nclumps, size=nlos)
     cofm[through] = centres[pick[through]]
-    return _finish("config3_%dcube_L1e5_%dlos_1kms_3lines" % (nside, nlos), box, 1.0, 1, pos,
-                   vel, temp, hh, {"HI": n_hi, "CIV": n_civ}, axis, cofm, [LYA, LYB, CIV])
+    w = _finish("config3_%dcube_L1e5_%dlos_1kms_3lines" % (nside, nlos), box, 1.0, 1, pos,
+                vel, temp, hh, {"HI": n_hi, "CIV": n_civ}, axis, cofm, [LYA, LYB, CIV])
+    w.line_class = through.astype(np.int8)
+    return w
 
 
 def config4(seed=4, nside=128, nlos=1024):
@@ -374,6 +379,7 @@ class DeviceWorkload:
     cofm: np.ndarray
     transitions: List[Transition] = field(default_factory=list)
     tautail: float = 1e-7
+    line_class: Optional[np.ndarray] = None   # 1: through a clump centre (config 3)
 
     @property
     def npart(self):
@@ -398,7 +404,7 @@ class DeviceWorkload:
                         pos=f(self.pos), vel=f(self.vel), temp=f(self.temp), hh=f(self.hh),
                         dens={k: f(v) for k, v in self.dens.items()}, axis=self.axis,
                         cofm=self.cofm, transitions=list(self.transitions),
-                        tautail=self.tautail)
+                        tautail=self.tautail, line_class=self.line_class)
 
 
 def generate_torch(config, seed=None, device="cuda", nside=None, nlos=None):
@@ -449,6 +455,7 @@ def generate_torch(config, seed=None, device="cuda", nside=None, nlos=None):
         dens64["CIV"] = 10 ** -4.5 * n_hi * delta1 ** 0.3
     del delta1
     rng = np.random.default_rng(seed)
+    line_class = None
     if "grid" in spec:
         axis, cofm = grid_sightlines(spec["grid"][0], spec["grid"][1], box)
     else:
@@ -462,6 +469,7 @@ def generate_torch(config, seed=None, device="cuda", nside=None, nlos=None):
             cen = centres.cpu().numpy()
             pick = rng.integers(0, nclumps, size=nl)
             cofm[through] = cen[pick[through]]
+            line_class = through.astype(np.int8)
         else:
             axis, cofm = random_sightlines(rng, nl, 1, box)
             cofm[:, 0] = 0.0
@@ -477,4 +485,4 @@ def generate_torch(config, seed=None, device="cuda", nside=None, nlos=None):
         temp=temp.to(torch.float32), hh=hh.to(torch.float32),
         dens={k: (v * rscale).to(torch.float32) for k, v in dens64.items()},
         axis=np.asarray(axis, dtype=np.int32), cofm=np.asarray(cofm, dtype=np.float64),
-        transitions=list(spec["lines"]))
+        transitions=list(spec["lines"]), line_class=line_class)

@@ -260,15 +260,25 @@ int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr
  * cannot call cudaMalloc (their host application's allocator owns the GPU
  * memory, or they run inside a loop that must not trigger the synchronisation
  * an allocation may imply).  This entry point has no counterpart in the
- * reference.  pos/vel/dens/temp/h/out are DEVICE pointers, axis/cofm HOST
- * pointers, stream a cudaStream_t (NULL = the default stream); precision is an
- * fsg_precision.  All scratch lives in one 64 MiB file-scope device array that
- * every GPU loading the library keeps until exit.  Limits: nlos <= 8192, about
- * 5.4 million sightline-particle pairs, nbins within the shared-memory
- * capacity (~14000 on GB300); larger calls return FSG_ERR_VALUE.  The first
- * call on a device looks up the array's address (do it before any stream
- * capture).  Calls share the array: they are serialised by a lock and complete
- * before returning; GPU work overlapping a call on the same array would race.
+ * reference.  pos/vel/dens/temp/h/out are DEVICE pointers of the current
+ * device (checked; another device's pointers return FSG_ERR_VALUE before any
+ * work is queued), axis/cofm HOST pointers, stream a cudaStream_t of the
+ * current device (NULL = the default stream); precision is an fsg_precision.
+ * All scratch lives in one 64 MiB file-scope device array that every GPU
+ * loading the library keeps until exit.  Limits, larger calls returning
+ * FSG_ERR_VALUE:
+ *   nlos <= 8192 sightlines;
+ *   about 5.4 million sightline-particle pairs (the rest of the array, 12
+ *   bytes per pair; checked after the pair count);
+ *   nbins within the shared-memory capacity of one deposit block: 16 bytes
+ *   per pixel beside the pair staging area, out of the device's opt-in
+ *   maximum less 2 KiB.  With GB300's 227 KiB: 14400 pixels in the FP64 form,
+ *   13760 for FP32 optical depths, 14016 for FP32 column densities.
+ * The first call on a device looks up the array's address (do it before any
+ * stream capture); the address is kept for the life of the process, so a
+ * cudaDeviceReset between calls is not supported.  Calls share the array:
+ * they are serialised by a lock and complete before returning (error returns
+ * included); GPU work overlapping a call on the same array would race.
  */
 int fsg_particle_interpolate_noalloc(int compute_tau, int nbins, int kernel, double box,
                                      double velfac, double atime, double lambda, double gamma,

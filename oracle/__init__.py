@@ -41,13 +41,27 @@ def build_port(force=False):
     return PORT_SO
 
 
-def build_ref(reference_root="/root/reference", force=False):
+def reference_root():
+    """Where the reference checkout is: $FSG_REFERENCE_ROOT, else a directory
+    named ``reference`` beside this repository.  Returns None when neither
+    holds the reference's ``fake_spectra`` sources."""
+    cands = [os.environ.get("FSG_REFERENCE_ROOT"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "fake_spectra", "part_int.cpp")):
+            return c
+    return None
+
+
+def build_ref(reference_root_dir=None, force=False):
     """Compile the unmodified reference sources, when they are present."""
-    if not os.path.isdir(os.path.join(reference_root, "fake_spectra")):
+    reference_root_dir = reference_root_dir or reference_root()
+    if not reference_root_dir or not os.path.isdir(os.path.join(reference_root_dir,
+                                                                "fake_spectra")):
         return None
     if force or not os.path.exists(REF_SO):
-        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), reference_root],
-                              stdout=subprocess.DEVNULL)
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"),
+                               reference_root_dir], stdout=subprocess.DEVNULL)
     return REF_SO
 
 
@@ -98,6 +112,11 @@ class Oracle:
             L.fsgo_kern_frac.restype = _c_d
             L.fsgo_assign_cells.argtypes = [_p, _p, _c_int, _c_int, _p, _c_d, _p]
             L.fsgo_assign_cells.restype = _c_int
+            L.fsgo_particle_interpolate_timed.argtypes = [_c_int, _c_int, _c_int] + \
+                [_c_d] * 8 + [_p] * 5 + [_c_ll, _p, _p, _c_int, _p, _p, _p]
+            L.fsgo_particle_interpolate_timed.restype = _c_int
+            L.fsgo_search_seconds.argtypes = [_p, _p, _c_ll, _p, _p, _c_int, _c_d, _p]
+            L.fsgo_search_seconds.restype = _c_d
         else:
             L.fsr_sph_cubic_kern_frac.argtypes = [_c_d] * 5
             L.fsr_sph_cubic_kern_frac.restype = _c_d
@@ -131,6 +150,43 @@ class Oracle:
         if count_evals:
             return out, int(ev.value)
         return out
+
+    def particle_interpolate_timed(self, compute_tau, nbins, kernel, box, velfac, atime, lam,
+                                   gamma, fosc, amumass, tautail, pos, vel, dens, temp, h, axis,
+                                   cofm):
+        """(out, search seconds, per-sightline deposit seconds of one thread); C
+        restatement only."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        dens = np.ascontiguousarray(dens, dtype=np.float32)
+        temp = np.ascontiguousarray(temp, dtype=np.float32)
+        h = np.ascontiguousarray(h, dtype=np.float32)
+        axis = np.ascontiguousarray(axis, dtype=np.int32)
+        cofm = np.ascontiguousarray(cofm, dtype=np.float64)
+        nlos = int(axis.shape[0])
+        out = np.zeros((nlos, int(nbins)), dtype=np.float64)
+        line_sec = np.zeros(max(nlos, 1), dtype=np.float64)
+        ts = _c_d(0.0)
+        rc = self.lib.fsgo_particle_interpolate_timed(
+            int(compute_tau), int(nbins), int(kernel), float(box), float(velfac), float(atime),
+            float(lam), float(gamma), float(fosc), float(amumass), float(tautail), _ptr(pos),
+            _ptr(vel), _ptr(dens), _ptr(temp), _ptr(h), int(pos.shape[0]), _ptr(axis),
+            _ptr(cofm), nlos, _ptr(out), ctypes.cast(ctypes.byref(ts), _p), _ptr(line_sec))
+        if rc != 0:
+            raise RuntimeError("oracle particle_interpolate failed with %d" % rc)
+        return out, float(ts.value), line_sec[:nlos]
+
+    def search_seconds(self, pos, h, axis, cofm, box):
+        """(wall seconds, pairs) of the pair search alone; C restatement only."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        h = np.ascontiguousarray(h, dtype=np.float32)
+        axis = np.ascontiguousarray(axis, dtype=np.int32)
+        cofm = np.ascontiguousarray(cofm, dtype=np.float64)
+        n = _c_ll(0)
+        sec = self.lib.fsgo_search_seconds(_ptr(pos), _ptr(h), int(pos.shape[0]), _ptr(axis),
+                                           _ptr(cofm), int(axis.shape[0]), float(box),
+                                           ctypes.cast(ctypes.byref(n), _p))
+        return float(sec), int(n.value)
 
     # -- pair lists ----------------------------------------------------------
     def near_particles(self, pos, h, axis, cofm, box):

@@ -3,9 +3,11 @@
 # read-only reference checkout) plus oracle/ref_shim.cpp into
 # oracle/_ref/libfsref.so, with the reference's own flags
 # (-O3 -ffast-math -fopenmp; reference Makefile:10, setup.py:57).
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+#   (default $FSG_REFERENCE_ROOT, else a "reference" directory beside this repository)
 set -e
-REF="${1:-/root/reference}"
+HERE0="$(cd "$(dirname "$0")" && pwd)"
+REF="${1:-${FSG_REFERENCE_ROOT:-$HERE0/../../reference}}"
 SRC="$REF/fake_spectra"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 if [ ! -f "$SRC/part_int.cpp" ]; then

@@ -902,17 +902,22 @@ int fsgo_assign_cells(const float *pos, const int32_t *part, int ncells, int axi
 /* ------------------------------------------------------------------ */
 /* ParticleInterp, part_int.cpp:20-84                                  */
 /* ------------------------------------------------------------------ */
-int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box, double velfac,
-                              double atime, double lambda, double gamma, double fosc,
-                              double amumass, double tautail, const float *pos, const float *vel,
-                              const float *dens, const float *temp, const float *h,
-                              long long npart, const int32_t *axis, const double *cofm, int nlos,
-                              double *out, long long *evals)
+/* The interpolation, optionally timed: *t_search receives the wall seconds of
+ * the pair search and line_sec[i] the seconds one thread spent depositing
+ * sightline i (either may be NULL). */
+static int interpolate_impl(int compute_tau, int nbins, int kernel, double box, double velfac,
+                            double lambda, double gamma, double fosc, double amumass,
+                            double tautail, const float *pos, const float *vel,
+                            const float *dens, const float *temp, const float *h,
+                            long long npart, const int32_t *axis, const double *cofm, int nlos,
+                            double *out, long long *evals, double *t_search, double *line_sec)
 {
-    (void)atime;
     memset(out, 0, sizeof(double) * (size_t)nlos * (size_t)nbins);
     csr_t c;
+    const double t0 = omp_get_wtime();
     build_csr(pos, h, npart, axis, cofm, nlos, box, &c);
+    if (t_search)
+        *t_search = omp_get_wtime() - t0;
     line_t l;
     line_init(&l, lambda, gamma, fosc, amumass, velfac, box, kernel, tautail);
     long long nev = 0;
@@ -920,6 +925,7 @@ int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box
     int nth = fsgo_get_threads();
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nth) reduction(+ : nev, failed)
     for (int i = 0; i < nlos; i++) {
+        const double tl0 = line_sec ? omp_get_wtime() : 0.0;
         const int ax = axis[i];
         double *row = &out[(size_t)i * nbins];
         const long long m = c.off[i + 1] - c.off[i];
@@ -946,17 +952,58 @@ int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box
                 add_colden(&l, row, nbins, d2, dens[ip], ppos, sm);
         }
         free(seg);
+        if (line_sec)
+            line_sec[i] = omp_get_wtime() - tl0;
     }
     if (evals)
         *evals = nev;
-    if (failed) {
-        free(c.off);
-        free(c.part);
-        free(c.dr2);
-        return -3;
-    }
     free(c.off);
     free(c.part);
     free(c.dr2);
-    return 0;
+    return failed ? -3 : 0;
+}
+
+int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box, double velfac,
+                              double atime, double lambda, double gamma, double fosc,
+                              double amumass, double tautail, const float *pos, const float *vel,
+                              const float *dens, const float *temp, const float *h,
+                              long long npart, const int32_t *axis, const double *cofm, int nlos,
+                              double *out, long long *evals)
+{
+    (void)atime;
+    return interpolate_impl(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                            amumass, tautail, pos, vel, dens, temp, h, npart, axis, cofm, nlos,
+                            out, evals, NULL, NULL);
+}
+
+int fsgo_particle_interpolate_timed(int compute_tau, int nbins, int kernel, double box,
+                                    double velfac, double atime, double lambda, double gamma,
+                                    double fosc, double amumass, double tautail,
+                                    const float *pos, const float *vel, const float *dens,
+                                    const float *temp, const float *h, long long npart,
+                                    const int32_t *axis, const double *cofm, int nlos,
+                                    double *out, double *t_search, double *line_sec)
+{
+    (void)atime;
+    return interpolate_impl(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
+                            amumass, tautail, pos, vel, dens, temp, h, npart, axis, cofm, nlos,
+                            out, NULL, t_search, line_sec);
+}
+
+/* Wall seconds of the pair search alone (IndexTable::get_near_particles,
+ * index_table.cpp:130-150) for these sightlines; *npairs receives the pair count. */
+double fsgo_search_seconds(const float *pos, const float *h, long long npart,
+                           const int32_t *axis, const double *cofm, int nlos, double box,
+                           long long *npairs)
+{
+    csr_t c;
+    const double t0 = omp_get_wtime();
+    build_csr(pos, h, npart, axis, cofm, nlos, box, &c);
+    const double dt = omp_get_wtime() - t0;
+    if (npairs)
+        *npairs = c.total;
+    free(c.off);
+    free(c.part);
+    free(c.dr2);
+    return dt;
 }

@@ -38,6 +38,20 @@ int fsgo_particle_interpolate(int compute_tau, int nbins, int kernel, double box
 
 /* Pair lists (index_table.cpp:130-150) as CSR by sightline, particles ascending.
  * Returns total pairs; part/dr2 are filled only if total <= cap. */
+/* The same with timing: *t_search = wall seconds of the pair search,
+ * line_sec[i] = one thread's seconds depositing sightline i (NULL = not wanted). */
+int fsgo_particle_interpolate_timed(int compute_tau, int nbins, int kernel, double box,
+                                    double velfac, double atime, double lambda, double gamma,
+                                    double fosc, double amumass, double tautail,
+                                    const float *pos, const float *vel, const float *dens,
+                                    const float *temp, const float *h, long long npart,
+                                    const int32_t *axis, const double *cofm, int nlos,
+                                    double *out, double *t_search, double *line_sec);
+/* Wall seconds of the pair search alone; *npairs receives the pair count. */
+double fsgo_search_seconds(const float *pos, const float *h, long long npart,
+                           const int32_t *axis, const double *cofm, int nlos, double box,
+                           long long *npairs);
+
 long long fsgo_near_particles(const float *pos, const float *h, long long npart,
                               const int32_t *axis, const double *cofm, int nlos, double box,
                               long long *counts, int32_t *part, double *dr2, long long cap);

@@ -67,11 +67,31 @@ def dense_tau(line, nbins, box, velfac, tautail, nlos, pair_line, pair_dr2, ppos
     half = nbins // 2
     k = torch.arange(-half, half, dtype=torch.float64)                      # pixel offsets
     z = zmax[:, None] + k[None, :]                                          # [P, K]
-    vouter = z * bintov - vel[:, None] + bintov / 2.
-    u = (vv[:, None, :] - vouter[:, :, None]) / btherm[:, None, None]      # [P, K, 7]
-    a3 = aa[:, None, None].expand_as(u)
-    H = _VoigtH.apply(u.reshape(-1), a3.reshape(-1)).reshape(u.shape)
-    tl = (amp * dens)[:, None] * deltav[:, None] * (H * w[:, None, :]).sum(-1) / velfac
+    vlow = z * bintov - vel[:, None]
+    # tau_kern_outer: midpoint (np = 1) or trapezoid sub-samples, per pair
+    with torch.no_grad():
+        half_b = btherm / 2.
+        npts = torch.where(bintov < half_b, torch.ones_like(half_b),
+                           2 * torch.ceil(bintov / half_b / 2) + 1).to(torch.int64)
+    S = torch.zeros(vlow.shape, dtype=torch.float64)
+    for n in torch.unique(npts).tolist():
+        sel = npts == n
+        if n == 1:
+            offs, wts = [0.5 * bintov], [1.0]
+        else:
+            dv = bintov / (n - 1)
+            offs = [i * dv for i in range(n)]
+            wts = [(0.5 if i in (0, n - 1) else 1.0) / (n - 1) for i in range(n)]
+        vl = vlow[sel]
+        acc = torch.zeros(vl.shape, dtype=torch.float64)
+        for off, wt in zip(offs, wts):
+            vouter = vl + off
+            u = (vv[sel][:, None, :] - vouter[:, :, None]) / btherm[sel][:, None, None]
+            a3 = aa[sel][:, None, None].expand_as(u)
+            H = _VoigtH.apply(u.reshape(-1), a3.reshape(-1)).reshape(u.shape)
+            acc = acc + wt * (H * w[sel][:, None, :]).sum(-1)
+        S = S.index_put((sel.nonzero()[:, 0],), acc)
+    tl = (amp * dens)[:, None] * deltav[:, None] * S / velfac
     # stop rule: forward from k = 0, backward from k = -1, each including the
     # first pixel below tautail
     with torch.no_grad():

@@ -5,7 +5,8 @@ reference C++ path (oracle/build_ref.sh -> oracle/_ref/libfsref.so), feeds it
 small seeded inputs and stores inputs + reference outputs as .npz files.  The
 fixtures then travel with the tests to machines without the reference.
 
-    python tests/golden/make_golden.py [/root/reference [voronoi]]
+    python tests/golden/make_golden.py [reference_root [voronoi]]   (default: $FSG_REFERENCE_ROOT,
+        else a "reference" directory beside this repository)
 """
 import os
 import sys
@@ -103,7 +104,10 @@ def voronoi_fixture(R, seed=21):
     return out
 
 
-def main(ref_root="/root/reference", only=None):
+def main(ref_root=None, only=None):
+    ref_root = ref_root or oracle.reference_root()
+    if not ref_root:
+        raise SystemExit("reference checkout not found: set FSG_REFERENCE_ROOT")
     oracle.build_ref(ref_root)
     R = oracle.ref()
     if R is None:

@@ -13,9 +13,9 @@ from conftest import ROOT
 def test_reference_arm_json_line():
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--config", "1", "--nside", "32", "--cpu-lines", "4", "--steps", "1",
-                        "--warmup", "1"], capture_output=True, text=True, timeout=600, env=env,
-                       cwd=ROOT)
+                        "--config", "3", "--nside", "32", "--nlos", "60", "--cpu-per-stratum", "1",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True,
+                       timeout=600, env=env, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -26,7 +26,7 @@ def test_reference_arm_json_line():
         assert k in d, k
     assert d["impl"] == "reference"
     assert d["value"] > 0 and d["unit"] == "pixels/s" and d["higher_is_better"] is True
-    assert d["steps"] == 1 and d["warmup"] == 1 and d["n_gpus"] == 1
+    assert d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
     assert "workload" in d["config"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
@@ -34,3 +34,6 @@ def test_reference_arm_json_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    est = cb["estimate"]
+    assert len(est["strata"]) == 6      # 3 axes x clump-centred or not
+    assert est["search_all_s"] > 0 and est["total_s_est"] > est["search_all_s"]
