@@ -29,6 +29,7 @@ EXPORTS = (
     "fsg_context_destroy",
     "fsg_context_set_stream",
     "fsg_context_stats",
+    "fsg_default_context_stats",
     "fsg_particle_interpolate",
     "fsg_particle_interpolate_device",
     "fsg_spectra_batch_device",
@@ -44,6 +45,10 @@ EXPORTS = (
     "fsg_mean_flux_device",
     "fsg_flux_histogram_device",
     "fsg_flux_power_device",
+    "fsg_tune_cache_file",
+    "fsg_tune_cache_lookup",
+    "fsg_tune_cache_store",
+    "fsg_tune_cache_clear",
 )
 
 _c_int = ctypes.c_int
@@ -56,7 +61,8 @@ _c_size = ctypes.c_size_t
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", _c_int), ("threads", _c_int), ("persistent", _c_int),
-                ("count_work", _c_int), ("no_far_tiles", _c_int), ("reserved", _c_int * 3)]
+                ("count_work", _c_int), ("no_far_tiles", _c_int), ("chunk", _c_int),
+                ("tune", _c_int), ("reserved", _c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -65,7 +71,23 @@ class Stats(ctypes.Structure):
                 ("evals_core", _c_i64), ("evals_wing", _c_i64), ("evals_other", _c_i64),
                 ("pixels", _c_i64), ("evals_wing_multipole", _c_i64),
                 ("samples_wing_path", _c_i64), ("samples_core_path", _c_i64),
-                ("samples_mixed_path", _c_i64)]
+                ("samples_mixed_path", _c_i64), ("launch_threads", _c_i32),
+                ("launch_chunk", _c_i32), ("launch_persistent", _c_i32),
+                ("launch_tuned", _c_i32), ("tune_ran", _c_i32), ("tune_candidates", _c_i32),
+                ("tune_sample_lines", _c_i32), ("reserved2", _c_i32),
+                ("tune_ms_default", _c_d), ("tune_ms_best", _c_d), ("ms_h2d", _c_d),
+                ("ms_d2h", _c_d)]
+
+
+class TuneKey(ctypes.Structure):
+    _fields_ = [(n, _c_i32) for n in ("sms", "precision", "compute_tau", "kernel", "nbins_b",
+                                      "pairs_med_b", "pairs_p99_b", "lines_b", "damp_b")]
+
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [("threads", _c_i32), ("chunk", _c_i32), ("persistent", _c_i32),
+                ("candidates", _c_i32), ("sample_lines", _c_i32), ("ms_default", _c_d),
+                ("ms_best", _c_d)]
 
 
 class Line(ctypes.Structure):
@@ -124,6 +146,7 @@ def load(path=None):
         L.fsg_context_destroy.restype = None
         L.fsg_context_set_stream.argtypes = [_p, _p]
         L.fsg_context_stats.argtypes = [_p, ctypes.POINTER(Stats)]
+        L.fsg_default_context_stats.argtypes = [ctypes.POINTER(Stats)]
         L.fsg_particle_interpolate.argtypes = _INTERP_ARGS
         L.fsg_particle_interpolate_device.argtypes = [_p] + _INTERP_ARGS
         L.fsg_spectra_batch_device.argtypes = ([_p, _c_int, _c_int] + [_c_d] * 4 + [_p] * 4 +
@@ -155,6 +178,12 @@ def load(path=None):
                                                 _c_size]
         L.fsg_flux_power_device.argtypes = [_p, _p, _c_i64, _c_i64, _c_d, _c_d, _c_d, _p, _p,
                                             _c_size]
+        L.fsg_tune_cache_file.argtypes = [ctypes.c_char_p, _p, _c_size]
+        L.fsg_tune_cache_lookup.argtypes = [ctypes.POINTER(TuneKey), ctypes.POINTER(TuneEntry)]
+        L.fsg_tune_cache_store.argtypes = [ctypes.POINTER(TuneKey), ctypes.POINTER(TuneEntry),
+                                           _p, _c_size]
+        L.fsg_tune_cache_clear.argtypes = []
+        L.fsg_tune_cache_clear.restype = None
         _lib = L
         return L
 
@@ -163,8 +192,14 @@ def errbuf():
     return ctypes.create_string_buffer(512)
 
 
-def make_options(precision="fp64", threads=0, persistent=-1, count_work=False, far_tiles=True):
+def make_options(precision="fp64", threads=0, persistent=-1, count_work=False, far_tiles=True,
+                 chunk=0, tune=0):
+    """fsg_options.  threads/chunk 0 and persistent -1 leave the launch to the
+    autotuner (FP32 form; tune 0 = cached choice, 1 = time again, -1 = library
+    defaults) or to the library defaults (FP64 form)."""
     o = Options()
+    o.chunk = int(chunk)
+    o.tune = int(tune)
     o.count_work = int(bool(count_work))
     o.no_far_tiles = int(not far_tiles)
     if precision in ("fp64", FSG_PREC_FP64):
@@ -201,14 +236,7 @@ class Context:
     def stats(self):
         s = Stats()
         self._lib.fsg_context_stats(self._h, ctypes.byref(s))
-        return {"npairs": int(s.npairs), "gpu_launches": int(s.gpu_launches),
-                "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
-                "ms_deposit": float(s.ms_deposit), "evals_core": int(s.evals_core),
-                "evals_wing": int(s.evals_wing), "evals_other": int(s.evals_other),
-                "pixels": int(s.pixels), "evals_wing_multipole": int(s.evals_wing_multipole),
-                "samples_wing_path": int(s.samples_wing_path),
-                "samples_core_path": int(s.samples_core_path),
-                "samples_mixed_path": int(s.samples_mixed_path)}
+        return _stats_dict(s)
 
     def close(self):
         if self._h:
@@ -222,6 +250,35 @@ class Context:
             pass
 
 
+def default_context_stats():
+    """Statistics of the library-owned context behind the host-pointer entry
+    points (the last fsg_particle_interpolate call on the current device)."""
+    s = Stats()
+    L = load()
+    if L.fsg_default_context_stats(ctypes.byref(s)) != FSG_OK:
+        return None
+    return _stats_dict(s)
+
+
+def _stats_dict(s):
+    return {"npairs": int(s.npairs), "gpu_launches": int(s.gpu_launches),
+            "fallback_lines": int(s.fallback_lines), "ms_search": float(s.ms_search),
+            "ms_deposit": float(s.ms_deposit), "evals_core": int(s.evals_core),
+            "evals_wing": int(s.evals_wing), "evals_other": int(s.evals_other),
+            "pixels": int(s.pixels), "evals_wing_multipole": int(s.evals_wing_multipole),
+            "samples_wing_path": int(s.samples_wing_path),
+            "samples_core_path": int(s.samples_core_path),
+            "samples_mixed_path": int(s.samples_mixed_path),
+            "launch": {"threads": int(s.launch_threads), "chunk": int(s.launch_chunk),
+                       "persistent": int(s.launch_persistent),
+                       "tuned": bool(s.launch_tuned)},
+            "tune": {"ran": bool(s.tune_ran), "candidates": int(s.tune_candidates),
+                     "sample_lines": int(s.tune_sample_lines),
+                     "ms_default": float(s.tune_ms_default),
+                     "ms_best": float(s.tune_ms_best)},
+            "ms_h2d": float(s.ms_h2d), "ms_d2h": float(s.ms_d2h)}
+
+
 def fma_peak_tflops(precision="fp32"):
     """Peak FMA throughput of the current GPU (TFLOP/s), own microbenchmark."""
     L = load()
@@ -230,3 +287,32 @@ def fma_peak_tflops(precision="fp32"):
     prec = FSG_PREC_FP64 if precision in ("fp64", FSG_PREC_FP64) else FSG_PREC_FP32
     raise_for(L.fsg_measure_fma_peak(prec, ctypes.byref(v), eb, 512), eb.value.decode())
     return float(v.value)
+
+
+def tune_cache_file(path):
+    """Name the autotuner's cache file (loaded now, appended to later); None/''
+    keeps the cache in the process only."""
+    L = load()
+    eb = errbuf()
+    raise_for(L.fsg_tune_cache_file(path.encode() if path else None, eb, 512),
+              eb.value.decode())
+
+
+def tune_cache_lookup(key):
+    """The cached fsg_tune_entry of a TuneKey as a dict, or None."""
+    e = TuneEntry()
+    if not load().fsg_tune_cache_lookup(ctypes.byref(key), ctypes.byref(e)):
+        return None
+    return {f: getattr(e, f) for f, _ in TuneEntry._fields_}
+
+
+def tune_cache_store(key, threads, chunk, persistent, ms_default=0.0, ms_best=0.0,
+                     candidates=0, sample_lines=0):
+    e = TuneEntry(threads, chunk, persistent, candidates, sample_lines, ms_default, ms_best)
+    eb = errbuf()
+    raise_for(load().fsg_tune_cache_store(ctypes.byref(key), ctypes.byref(e), eb, 512),
+              eb.value.decode())
+
+
+def tune_cache_clear():
+    load().fsg_tune_cache_clear()

@@ -17,11 +17,14 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <numeric>
 #include <string>
+#include <tuple>
 #include <vector>
 
 using namespace fsg;
@@ -82,7 +85,9 @@ struct fsg_context {
     DevBuf flag, tcount, tstart, tsums, idx;                 // _near_lines
     DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
     DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
+    DevBuf tune_order;                                       // autotuner sample
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t cp[2] = {nullptr, nullptr};   // copy timing of the host-pointer entries
     // host mirrors
     std::vector<long long> h_off;
     std::vector<int> h_order;
@@ -118,7 +123,7 @@ struct fsg_context {
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
-                          &ffft, &fpower, &vseg, &vscratch, &vcofm};
+                          &ffft, &fpower, &vseg, &vscratch, &vcofm, &tune_order};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -342,30 +347,31 @@ long long near_lines(fsg_context *c, const Particles &p, int *out)
 
 // get_mean_flux_scale (py_module.cpp:235-260): Newton-Raphson on the scale of
 // tau until the mean of exp(-scale tau) over the pixels with tau <= thresh is
-// mean_flux_desired; the same update and stopping rule, sums on the device.
+// mean_flux_desired; the same update and stopping rule.  The scale stays on
+// the device between passes: the host queues NEWTON_BATCH passes, then reads
+// whether they converged (passes queued after convergence return at once).
+constexpr int NEWTON_BATCH = 8;
+
 double mean_flux_scale(fsg_context *c, const double *tau, long long n, double mfd, double tol,
                        double thresh)
 {
     cudaStream_t s = c->stream;
     auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
-    auto *out = (double *)c->ensure(c->fout, sizeof(double) * 4);
-    double scale, newscale = 1.0;
-    int iterations = 0;
-    do {
-        scale = newscale;
-        double h[3];
-        launch_flux_moments(tau, n, scale, thresh, part, out, s);
-        c->stats.gpu_launches += 2;
+    auto *state = (double *)c->ensure(c->fout, sizeof(double) * 4);
+    const double init[4] = {1.0, 1.0, 0.0, 0.0};
+    cuda_check(cudaMemcpyAsync(state, init, sizeof init, cudaMemcpyHostToDevice, s), "H2D");
+    double h[4] = {0, 0, 0, 0};
+    for (;;) {
+        launch_newton_passes(tau, n, mfd, tol, thresh, NEWTON_BATCH, part, state, s);
+        c->stats.gpu_launches += 2 * NEWTON_BATCH;
         cuda_check(cudaGetLastError(), "flux moments launch");
-        cuda_check(cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, s), "read");
+        cuda_check(cudaMemcpyAsync(h, state, sizeof h, cudaMemcpyDeviceToHost, s), "read");
         cuda_check(cudaStreamSynchronize(s), "flux moments");
-        newscale = scale + (h[0] - mfd * h[2]) / h[1];
-        if (newscale <= 0)
-            newscale = 1e-10;
-        if (++iterations > 10000)
+        if (h[2] != 0.0)
+            return h[1];
+        if (h[3] > 10000)
             fail(FSG_ERR_VALUE, "mean-flux rescaling did not converge in 10000 iterations");
-    } while (fabs(newscale - scale) > tol * newscale);
-    return newscale;
+    }
 }
 
 double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale)
@@ -383,6 +389,8 @@ double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale
 }
 
 DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt);
+void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, const Particles &p,
+                  const PairLists &pl, double *out, DepositLaunch &cfg);
 
 // 3. deposit into out (device, nlos*nbins)
 void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
@@ -391,19 +399,22 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     cudaStream_t s = c->stream;
     const int nlos = c->nlos;
     const size_t nout = (size_t)nlos * lp.nbins;
-    cuda_check(cudaEventRecord(c->ev[2], s), "event");
-    if (nout)
-        cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * nout, s), "memset out");
     c->stats.fallback_lines = 0;
+    c->stats.tune_ran = 0;
     if (nout == 0 || c->npairs == 0) {
-        cuda_check(cudaEventRecord(c->ev[3], s), "event");
+        if (nout)
+            cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * nout, s), "memset out");
         cuda_check(cudaStreamSynchronize(s), "deposit");
         c->stats.ms_deposit = 0;
         return;
     }
     PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p,
                  seg};
-    const DepositLaunch cfg = deposit_config(c, lp, opt);
+    DepositLaunch cfg = deposit_config(c, lp, opt);
+    // the tuner times candidates on sample rows of `out`, which is cleared below
+    apply_tuning(c, lp, opt, p, pl, out, cfg);
+    cuda_check(cudaEventRecord(c->ev[2], s), "event");
+    cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * nout, s), "memset out");
     unsigned long long *gacc = nullptr;
     if (!cfg.smem_mode) {
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
@@ -480,6 +491,8 @@ LineParams make_line_params(int compute_tau, int nbins, int kernel, double box, 
     return lp;
 }
 
+void finish_config(fsg_context *c, const LineParams &lp, DepositLaunch &cfg);
+
 // Launch configuration of the deposit for this call.
 DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt)
 {
@@ -491,19 +504,267 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
     const bool vor = lp.kernel == VORONOI;
     if (vor)
         cfg.precision = FSG_PREC_FP64;
-    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
-    cfg.threads = (opt && opt->threads > 0 && !vor) ? opt->threads : tmax;
+    // FP32 optical depths have 768- and 1024-thread kernel builds
+    const int tdef = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
+    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : (lp.compute_tau ? 1024 : 512);
+    cfg.threads = (opt && opt->threads > 0 && !vor) ? opt->threads : tdef;
     if (cfg.threads % 32 || cfg.threads > tmax)
         fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
-    cfg.tiles = !(opt && opt->no_far_tiles);
+    cfg.tiles = cfg.tiles_asked = !(opt && opt->no_far_tiles);
+    cfg.chunk = (opt && cfg.precision == FSG_PREC_FP32) ? opt->chunk : 0;
+    if (cfg.chunk < 0 || cfg.chunk > 32)
+        fail(FSG_ERR_VALUE, "chunk must be between 1 and 32 (0 = tuned or default)");
     deposit_plan(cfg, lp.compute_tau, lp.nbins);
     cfg.persistent = (opt && opt->persistent >= 0 && !vor)
                          ? opt->persistent : (cfg.precision == FSG_PREC_FP32 ? 1 : 0);
+    finish_config(c, lp, cfg);
+    c->stats.launch_tuned = 0;
+    return cfg;
+}
+
+// ---------------------------------------------------------------- autotuner
+// The FP32 deposit's launch (threads per block, pairs staged per warp, queue
+// mode) is chosen by timing candidates on a sample of the call's own
+// sightlines, once per workload class (fsg_tune_key), and cached: in the
+// process, and in a text file when one is named (fsg_tune_cache_file or the
+// FSG_TUNE_CACHE environment variable).  Every candidate gives the same output
+// bits (integer accumulation with a scale that does not depend on the launch),
+// so the choice changes the speed only.
+struct TuneKeyLess {
+    bool operator()(const fsg_tune_key &a, const fsg_tune_key &b) const
+    {
+        return std::tie(a.sms, a.precision, a.compute_tau, a.kernel, a.nbins_b, a.pairs_med_b,
+                        a.pairs_p99_b, a.lines_b, a.damp_b) <
+               std::tie(b.sms, b.precision, b.compute_tau, b.kernel, b.nbins_b, b.pairs_med_b,
+                        b.pairs_p99_b, b.lines_b, b.damp_b);
+    }
+};
+
+std::mutex g_tune_mu;
+std::map<fsg_tune_key, fsg_tune_entry, TuneKeyLess> g_tune;
+std::string g_tune_file;
+bool g_tune_env_read = false;
+
+constexpr const char *TUNE_FILE_TAG = "fsg-tune-v1";
+
+// Reads the entries of a cache file (lines that do not parse are skipped);
+// the caller holds g_tune_mu.
+void tune_load_locked(const std::string &path)
+{
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f)
+        return;
+    char line[512];
+    while (fgets(line, sizeof line, f)) {
+        char tag[32];
+        fsg_tune_key k{};
+        fsg_tune_entry e{};
+        const int n = sscanf(line, "%31s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %lf %lf", tag,
+                             &k.sms, &k.precision, &k.compute_tau, &k.kernel, &k.nbins_b,
+                             &k.pairs_med_b, &k.pairs_p99_b, &k.lines_b, &k.damp_b, &e.threads,
+                             &e.chunk, &e.persistent, &e.candidates, &e.sample_lines,
+                             &e.ms_default, &e.ms_best);
+        if (n == 17 && strcmp(tag, TUNE_FILE_TAG) == 0 && e.threads > 0 && e.threads % 32 == 0 &&
+            e.chunk >= 1 && e.chunk <= 32 && (e.persistent == 0 || e.persistent == 1))
+            g_tune[k] = e;
+    }
+    fclose(f);
+}
+
+void tune_env_locked()
+{
+    if (g_tune_env_read)
+        return;
+    g_tune_env_read = true;
+    const char *env = getenv("FSG_TUNE_CACHE");
+    if (env && *env && g_tune_file.empty()) {
+        g_tune_file = env;
+        tune_load_locked(g_tune_file);
+    }
+}
+
+bool tune_store_locked(const fsg_tune_key &k, const fsg_tune_entry &e)
+{
+    g_tune[k] = e;
+    if (g_tune_file.empty())
+        return true;
+    FILE *f = fopen(g_tune_file.c_str(), "a");
+    if (!f)
+        return false;
+    fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %.6f %.6f\n", TUNE_FILE_TAG, k.sms,
+            k.precision, k.compute_tau, k.kernel, k.nbins_b, k.pairs_med_b, k.pairs_p99_b,
+            k.lines_b, k.damp_b, e.threads, e.chunk, e.persistent, e.candidates, e.sample_lines,
+            e.ms_default, e.ms_best);
+    fclose(f);
+    return true;
+}
+
+int floor_log2x2(double v) { return (int)std::floor(2.0 * std::log2(v)); }
+
+fsg_tune_key tune_key(fsg_context *c, const LineParams &lp, int precision)
+{
+    fsg_tune_key k{};
+    cudaDeviceGetAttribute(&k.sms, cudaDevAttrMultiProcessorCount, c->device);
+    k.precision = precision;
+    k.compute_tau = lp.compute_tau;
+    k.kernel = lp.kernel;
+    k.nbins_b = floor_log2x2(std::max(1, lp.nbins));
+    std::vector<long long> cnt((size_t)c->nlos);
+    for (int i = 0; i < c->nlos; i++)
+        cnt[i] = c->h_off[i + 1] - c->h_off[i];
+    std::sort(cnt.begin(), cnt.end());
+    const auto q = [&](double f) { return cnt[(size_t)std::min<double>(f * cnt.size(),
+                                                                       cnt.size() - 1)]; };
+    k.pairs_med_b = floor_log2x2(1.0 + (double)q(0.5));
+    k.pairs_p99_b = floor_log2x2(1.0 + (double)q(0.99));
+    k.lines_b = (int)std::floor(std::log2((double)std::max(1, c->nlos)));
+    k.damp_b = lp.compute_tau ? floor_log2x2(std::max(1e-300, lp.voigt_fac / lp.bfac)) : 0;
+    return k;
+}
+
+// The grid of a configuration: resident CTAs on every SM, at most one per sightline.
+void finish_config(fsg_context *c, const LineParams &lp, DepositLaunch &cfg)
+{
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     const int per_sm = std::max(1, deposit_resident_ctas(cfg, lp.compute_tau, lp.nbins));
     cfg.grid = std::min(c->nlos, sms * per_sm);
-    return cfg;
+}
+
+// Times the candidate launches on a sample of the call's sightlines (every
+// k-th of the descending pair-count order, about four sightlines per resident
+// CTA so that the queue's balance resembles the full call's) and returns the
+// fastest.  The sample rows of `out` are overwritten.
+fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particles &p,
+                            const PairLists &pl, double *out, const DepositLaunch &base)
+{
+    cudaStream_t s = c->stream;
+    const int nlos = c->nlos;
+    const int want = std::max(64, 4 * base.grid);
+    const int nsamp = std::min(nlos, want);
+    std::vector<int> order((size_t)nsamp);
+    for (int i = 0; i < nsamp; i++)
+        order[i] = c->h_order[(size_t)((double)i * nlos / nsamp)];
+    int *d_order = (int *)c->ensure(c->tune_order, sizeof(int) * (size_t)nsamp);
+    cuda_check(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * nsamp,
+                               cudaMemcpyHostToDevice, s), "upload tuning sample");
+    auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
+    auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
+    auto *nbad = (int *)c->ensure(c->nbad, sizeof(int));
+    auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
+    unsigned long long *gacc = nullptr;
+    if (!base.smem_mode)
+        gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 *
+                                                            (size_t)nlos * lp.nbins);
+    struct Cand {
+        int threads, chunk, persistent;
+    };
+    std::vector<Cand> cands;
+    if (lp.compute_tau)
+        cands = {{512, 8, 1}, {512, 4, 1}, {512, 16, 1}, {512, 8, 0}, {256, 8, 1},
+                 {768, 8, 1}, {768, 4, 1}, {1024, 4, 1}, {1024, 8, 1}};
+    else
+        cands = {{512, 32, 1}, {512, 16, 1}, {512, 8, 1}, {512, 32, 0}, {256, 32, 1},
+                 {256, 16, 1}};
+    fsg_tune_entry best{};
+    best.ms_best = 1e300;
+    best.sample_lines = nsamp;
+    for (const Cand &cd : cands) {
+        DepositLaunch cfg = base;
+        cfg.threads = cd.threads;
+        cfg.chunk = cd.chunk;
+        cfg.persistent = cd.persistent;
+        cfg.tiles = base.tiles_asked;
+        deposit_plan(cfg, lp.compute_tau, lp.nbins);
+        if (cfg.smem_mode != base.smem_mode || cfg.tiles != base.tiles)
+            continue;   // only launches that keep the default's on-chip layout
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+        const int per_sm = std::max(1, deposit_resident_ctas(cfg, lp.compute_tau, lp.nbins));
+        cfg.grid = std::min(nsamp, sms * per_sm);
+        float ms_min = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
+            cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int), s), "memset");
+            cuda_check(cudaEventRecord(c->ev[2], s), "event");
+            c->stats.gpu_launches += launch_deposit(lp, c->tables, p, pl, d_order, nsamp, out,
+                                                    ticket, bad, nbad, err, gacc, nullptr, cfg,
+                                                    s);
+            cuda_check(cudaGetLastError(), "tuning launch");
+            cuda_check(cudaEventRecord(c->ev[3], s), "event");
+            cuda_check(cudaEventSynchronize(c->ev[3]), "tuning");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+            ms_min = std::min(ms_min, ms);
+        }
+        best.candidates++;
+        if (cd.threads == base.threads && cd.chunk == base.chunk &&
+            cd.persistent == base.persistent)
+            best.ms_default = ms_min;
+        if (ms_min < best.ms_best) {
+            best.ms_best = ms_min;
+            best.threads = cd.threads;
+            best.chunk = cd.chunk;
+            best.persistent = cd.persistent;
+        }
+    }
+    if (best.candidates == 0) {   // nothing kept the layout: the defaults
+        best.threads = base.threads;
+        best.chunk = base.chunk;
+        best.persistent = base.persistent;
+        best.ms_best = best.ms_default = 0.0;
+    }
+    return best;
+}
+
+void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, const Particles &p,
+                  const PairLists &pl, double *out, DepositLaunch &cfg)
+{
+    c->stats.launch_threads = cfg.threads;
+    c->stats.launch_chunk = cfg.chunk;
+    c->stats.launch_persistent = cfg.persistent;
+    c->stats.launch_tuned = 0;
+    const int mode = opt ? opt->tune : 0;
+    if (cfg.precision != FSG_PREC_FP32 || lp.kernel == VORONOI || mode < 0 || !opt ||
+        opt->count_work || opt->threads > 0 || opt->chunk > 0 || opt->persistent >= 0 ||
+        c->nlos <= 0 || pl.seg)
+        return;
+    const fsg_tune_key key = tune_key(c, lp, cfg.precision);
+    fsg_tune_entry e{};
+    bool have = false;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_env_locked();
+        auto it = g_tune.find(key);
+        if (it != g_tune.end() && mode == 0) {
+            e = it->second;
+            have = true;
+        }
+    }
+    if (!have) {
+        e = tune_deposit(c, lp, p, pl, out, cfg);
+        c->stats.tune_ran = 1;
+        c->stats.tune_candidates = e.candidates;
+        c->stats.tune_sample_lines = e.sample_lines;
+        c->stats.tune_ms_default = e.ms_default;
+        c->stats.tune_ms_best = e.ms_best;
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_store_locked(key, e);
+    }
+    DepositLaunch t = cfg;
+    t.threads = e.threads;
+    t.chunk = e.chunk;
+    t.persistent = e.persistent;
+    t.tiles = cfg.tiles_asked;
+    deposit_plan(t, lp.compute_tau, lp.nbins);
+    if (t.smem_mode != cfg.smem_mode || t.tiles != cfg.tiles)
+        return;   // a cached choice that does not fit this call's layout
+    finish_config(c, lp, t);
+    cfg = t;
+    c->stats.launch_threads = cfg.threads;
+    c->stats.launch_chunk = cfg.chunk;
+    c->stats.launch_persistent = cfg.persistent;
+    c->stats.launch_tuned = 1;
 }
 
 // The batched form (fsg_spectra_batch_device): every deposit of the call in
@@ -519,8 +780,12 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
         return;
     PairLists pl{(const long long *)c->off.p, (const int *)c->part.p, (const double *)c->dr2.p};
     std::vector<DepositLaunch> cfgs;
-    for (const LineParams &lp : lps)
-        cfgs.push_back(deposit_config(c, lp, opt));
+    for (size_t k = 0; k < lps.size(); k++) {
+        cfgs.push_back(deposit_config(c, lps[k], opt));
+        Particles p = p0;
+        p.dens = dens[k];
+        apply_tuning(c, lps[k], opt, p, pl, outs[k], cfgs.back());
+    }
     unsigned long long *gacc = nullptr;
     if (!cfgs[0].smem_mode)
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
@@ -563,6 +828,8 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
         put(cfgs[k].threads);
         put(cfgs[k].persistent);
         put(cfgs[k].grid);
+        put(cfgs[k].chunk);
+        put(cfgs[k].tiles);
     }
     cudaStream_t s = c->own;
     cuda_check(cudaStreamSynchronize(c->stream), "sync caller stream");
@@ -617,6 +884,8 @@ void ctx_init(fsg_context *c, int device)
     cuda_check(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
     c->stream = c->own;
     for (auto &e : c->ev)
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    for (auto &e : c->cp)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
 }
 
@@ -816,6 +1085,9 @@ void fsg_context_destroy(fsg_context *ctx)
     for (auto &e : ctx->ev)
         if (e)
             cudaEventDestroy(e);
+    for (auto &e : ctx->cp)
+        if (e)
+            cudaEventDestroy(e);
     if (ctx->graph)
         cudaGraphExecDestroy(ctx->graph);
     if (ctx->own)
@@ -838,6 +1110,20 @@ int fsg_context_stats(const fsg_context *ctx, fsg_stats *out)
     if (!ctx || !out)
         return FSG_ERR_VALUE;
     *out = ctx->stats;
+    return FSG_OK;
+}
+
+int fsg_default_context_stats(fsg_stats *out)
+{
+    if (!out)
+        return FSG_ERR_VALUE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return FSG_ERR_VALUE;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if (!g_default[dev])
+        return FSG_ERR_VALUE;
+    *out = g_default[dev]->stats;
     return FSG_OK;
 }
 
@@ -886,20 +1172,29 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         };
         Particles p;
         p.n = npart;
+        cuda_check(cudaEventRecord(c->cp[0], s), "event");
         p.pos = up(c->pos, pos, n3);
         p.dens = up(c->dens, dens, n1);
         p.hh = up(c->hh, h, n1);
         p.vel = compute_tau ? up(c->vel, vel, n3) : nullptr;
         p.temp = compute_tau ? up(c->temp, temp, n1) : nullptr;
+        cuda_check(cudaEventRecord(c->cp[1], s), "event");
         const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
         double *dout = (double *)c->ensure(c->out, nout);
         PreTouch touch(out, nout);
         run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
                         tautail, p, axis, cofm, nlos, dout, opt);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
+        c->stats.ms_h2d = ms;
         touch.wait();
+        cuda_check(cudaEventRecord(c->cp[0], s), "event");
         if (nout)
             cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
+        cuda_check(cudaEventRecord(c->cp[1], s), "event");
         cuda_check(cudaStreamSynchronize(s), "D2H");
+        cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
+        c->stats.ms_d2h = ms;
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);
@@ -1320,6 +1615,65 @@ int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, in
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);
     }
+}
+
+int fsg_tune_cache_file(const char *path, char *errbuf, size_t errlen)
+{
+    try {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_env_read = true;   // an explicit file replaces FSG_TUNE_CACHE
+        g_tune_file = path ? path : "";
+        if (!g_tune_file.empty()) {
+            FILE *f = fopen(g_tune_file.c_str(), "a");
+            if (!f)
+                fail(FSG_ERR_VALUE, "cannot open the tuning cache file %s", g_tune_file.c_str());
+            fclose(f);
+            tune_load_locked(g_tune_file);
+        }
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+int fsg_tune_cache_lookup(const fsg_tune_key *key, fsg_tune_entry *entry)
+{
+    if (!key || !entry)
+        return 0;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_env_locked();
+    auto it = g_tune.find(*key);
+    if (it == g_tune.end())
+        return 0;
+    *entry = it->second;
+    return 1;
+}
+
+int fsg_tune_cache_store(const fsg_tune_key *key, const fsg_tune_entry *entry, char *errbuf,
+                         size_t errlen)
+{
+    try {
+        if (!key || !entry)
+            fail(FSG_ERR_VALUE, "key and entry must not be NULL");
+        if (entry->threads <= 0 || entry->threads % 32 || entry->threads > 1024 ||
+            entry->chunk < 1 || entry->chunk > 32 ||
+            (entry->persistent != 0 && entry->persistent != 1))
+            fail(FSG_ERR_VALUE, "not a valid launch: threads a multiple of 32 up to 1024, "
+                                "chunk 1..32, persistent 0 or 1");
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_env_locked();
+        if (!tune_store_locked(*key, *entry))
+            fail(FSG_ERR_VALUE, "cannot append to the tuning cache file %s", g_tune_file.c_str());
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
+void fsg_tune_cache_clear(void)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune.clear();
 }
 
 int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr2, int sorted,

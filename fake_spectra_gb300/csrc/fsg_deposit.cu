@@ -76,6 +76,48 @@ __device__ __forceinline__ T quintic_kernel(T q)  // singleabs.h:31-42
     return norm * ((T)243 * t * t * t * t * t);
 }
 
+// FP64 forms with every product and sum rounded on its own (no fused
+// multiply-add), in the reference's order of operations.  Near the edge of the
+// kernel support, 1 - q cancels and amplifies the last-bit difference a fused
+// operation makes (up to 1e-9 relative in a column-density pixel fed only by
+// such tails); unfused, each contribution equals the reference's double
+// arithmetic.
+__device__ __forceinline__ double cubic_kernel_rn(double q)   // singleabs.h:17-26
+{
+    const double norm = 32. / 4 / PI_D;
+    if (q >= 1.0)
+        return 0.0;
+    if (q < 0.5) {
+        const double q6 = __dmul_rn(6.0, q), q6q = __dmul_rn(q6, q);
+        return __dmul_rn(norm, __dadd_rn(__dsub_rn(1.0, q6q), __dmul_rn(q6q, q)));
+    }
+    const double t = __dsub_rn(1.0, q);
+    return __dmul_rn(norm, __dmul_rn(__dmul_rn(__dmul_rn(2.0, t), t), t));
+}
+
+__device__ __forceinline__ double quintic_kernel_rn(double q)   // singleabs.h:31-42
+{
+    const double norm = 9. / 40 / PI_D;
+    if (q >= 1.0)
+        return 0.0;
+    if (q < 1. / 3) {
+        const double q90 = __dmul_rn(__dmul_rn(90.0, q), q);
+        const double q405_4 = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(405.0, q), q), q), q);
+        const double q405_5 = __dmul_rn(q405_4, q);
+        const double r = __dsub_rn(__dadd_rn(__dsub_rn(11.0, q90), q405_4), q405_5);
+        return __dmul_rn(__dmul_rn(norm, 6.0), r);
+    }
+    if (q < 2. / 3) {
+        const double a = __dsub_rn(3.0, __dmul_rn(3.0, q)), b = __dsub_rn(2.0, __dmul_rn(3.0, q));
+        const double a5 = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(a, a), a), a), a);
+        const double b5 = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(6.0, b), b), b), b), b);
+        return __dmul_rn(norm, __dsub_rn(a5, b5));
+    }
+    const double t = __dsub_rn(1.0, q);
+    return __dmul_rn(norm, __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(243.0, t), t), t), t),
+                                     t));
+}
+
 // Weight of one line-of-sight node in tau_kern_inner (singleabs.h:158-163):
 // unknown kernel ids get no weight factor.
 template <class T>
@@ -88,6 +130,18 @@ __device__ __forceinline__ T node_weight(int kernel, T q)
     if (kernel == TOP_HAT)
         return (T)(3. / 4. / PI_D);
     return (T)1;
+}
+
+template <>
+__device__ __forceinline__ double node_weight<double>(int kernel, double q)
+{
+    if (kernel == SPH_CUBIC)
+        return cubic_kernel_rn(q);
+    if (kernel == SPH_QUINTIC)
+        return quintic_kernel_rn(q);
+    if (kernel == TOP_HAT)
+        return 3. / 4. / PI_D;
+    return 1.0;
 }
 
 __device__ __forceinline__ double kernel_max(int kernel)
@@ -129,6 +183,38 @@ __device__ T kern_frac(int kernel, T zlow, T zhigh, T smooth, T dr2, T zrange)
     if (kernel == VORONOI)   // arepo_kern_frac, absorption.cpp:129-134: overlap length
         return d > (T)0 ? d : (T)0;
     return (T)(3. / 4. / PI_D) * (d > (T)0 ? d : (T)0);
+}
+
+// FP64: unfused, in the reference's order (see cubic_kernel_rn)
+template <>
+__device__ double kern_frac<double>(int kernel, double zlow, double zhigh, double smooth,
+                                    double dr2, double zrange)
+{
+    if (zlow < -zrange)
+        zlow = -zrange;
+    if (zhigh > zrange)
+        zhigh = zrange;
+    if (kernel == SPH_CUBIC || kernel == SPH_QUINTIC) {
+        if (zlow > zhigh)
+            return 0.0;
+        const bool cub = (kernel == SPH_CUBIC);
+        const auto kern = [cub](double z, double dr2_, double smooth_) {
+            const double q = __ddiv_rn(__dsqrt_rn(__dadd_rn(dr2_, __dmul_rn(z, z))), smooth_);
+            return cub ? cubic_kernel_rn(q) : quintic_kernel_rn(q);
+        };
+        double total = kern(zlow, dr2, smooth) / 2.0;
+        const double deltaz = __dsub_rn(zhigh, zlow) / NGRID;
+        for (int i = 1; i < NGRID; ++i) {
+            const double zz = __dadd_rn(__dmul_rn((double)i, deltaz), zlow);
+            total = __dadd_rn(total, kern(zz, dr2, smooth));
+        }
+        total = __dadd_rn(total, kern(zhigh, dr2, smooth) / 2.0);
+        return __dmul_rn(deltaz, total);
+    }
+    const double d = __dsub_rn(zhigh, zlow);
+    if (kernel == VORONOI)
+        return d > 0.0 ? d : 0.0;
+    return __dmul_rn(3. / 4. / PI_D, d > 0.0 ? d : 0.0);
 }
 
 // ------------------------------------------------- 128-bit fixed point
@@ -394,15 +480,19 @@ struct Tau64 {
         const double vdr2 = vor ? lp.velfac * in.dr2 : (lp.velfac * in.dr2) * lp.velfac;
         const double vsmooth = lp.velfac * (double)in.smooth;
         aa = lp.voigt_fac / btherm;
-        double vhigh = (vsmooth * vsmooth > vdr2 ? sqrt(vsmooth * vsmooth - vdr2) : 0);
+        // node positions and kernel weights unfused, in the reference's order
+        // (singleabs.h:85, 150-156; see cubic_kernel_rn)
+        const double vs2 = __dmul_rn(vsmooth, vsmooth);
+        double vhigh = (vs2 > vdr2 ? __dsqrt_rn(__dsub_rn(vs2, vdr2)) : 0);
         if (vor)   // singleabs.h:85-89
             vhigh = (vdr2 > 0 && vsmooth > 0) ? (vsmooth - vdr2) / 2. : 0.;
         deltav = 2. * vhigh / NGRID;
 #pragma unroll
         for (int i = 1; i < NGRID; ++i) {
-            const double v = i * deltav - vhigh;
+            const double v = __dsub_rn(__dmul_rn((double)i, deltav), vhigh);
             vv[i - 1] = v;
-            w[i - 1] = node_weight<double>(lp.kernel, sqrt(vdr2 + v * v) / vsmooth);
+            w[i - 1] = node_weight<double>(
+                lp.kernel, __ddiv_rn(__dsqrt_rn(__dadd_rn(vdr2, __dmul_rn(v, v))), vsmooth));
         }
         const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
         ampd = amp * (double)in.dens;
@@ -891,8 +981,9 @@ struct Colden {
 
     __device__ __forceinline__ double value64(long long z) const
     {
-        const double plow = (boxtokpc * (double)z - pos1);
-        return dens * kern_frac<double>(kernel, plow, plow + boxtokpc, smooth, dr2, zrange);
+        const double plow = __dsub_rn(__dmul_rn(boxtokpc, (double)z), pos1);
+        return __dmul_rn(dens, kern_frac<double>(kernel, plow, __dadd_rn(plow, boxtokpc), smooth,
+                                                 dr2, zrange));
     }
 };
 
@@ -984,21 +1075,67 @@ __device__ __forceinline__ double colden_pair_bound32(const LineParams &lp, cons
 }
 
 // ------------------------------------------------------------ reductions
-__device__ __forceinline__ double block_sum(double v, double *scratch)
+// Block-wide upper bound of a sightline's total, sum_p b_p over its pairs
+// [e0, e1), computed so that it does not depend on how the pairs are spread
+// over the threads: with e = max_p ilogb(b_p) (an integer maximum),
+//   B = 2^(e - 30) x sum_p ceil(b_p 2^(30 - e)),
+// a sum of integers below 2^31 each, exact in 64 bits for up to 2^32 pairs.
+// The fixed-point scale follows from ilogb(B), so the output bits are the same
+// for every block size, chunk size and queue mode.  Returns +inf when a bound
+// is not finite (the sightline then goes to the non-finite fallback) and 0 when
+// every bound is 0.  `bound(e)` is evaluated twice per pair.
+struct BoundScratch {
+    int em[32];
+    unsigned long long q[32];
+};
+
+template <class BoundFn>
+__device__ __forceinline__ double order_free_bound(long long e0, long long e1, BoundFn bound,
+                                                   BoundScratch *sc)
 {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int NONE = -2147483647;
+    int em = NONE;
+    bool bad = false;
+    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const double b = bound(e);
+        if (!isfinite(b))
+            bad = true;
+        else if (b > 0.0)
+            em = max(em, ilogb(b));
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+    bad = __any_sync(0xffffffffu, bad);
     __syncthreads();
     if (lane == 0)
-        scratch[warp] = v;
+        sc->em[warp] = bad ? 2147483647 : em;
     __syncthreads();
-    const int nw = blockDim.x >> 5;
-    double t = 0;
+    int eall = NONE;
     for (int i = 0; i < nw; i++)
-        t += scratch[i];
-    return t;
+        eall = max(eall, sc->em[i]);
+    if (eall == 2147483647)
+        return __longlong_as_double(0x7ff0000000000000ll);
+    if (eall == NONE)
+        return 0.0;
+    unsigned long long q = 0;
+    for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const double b = bound(e);
+        if (b > 0.0)
+            q += (unsigned long long)ceil(scalbn(b, 30 - eall));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+    __syncthreads();
+    if (lane == 0)
+        sc->q[warp] = q;
+    __syncthreads();
+    unsigned long long Q = 0;
+    for (int i = 0; i < nw; i++)
+        Q += sc->q[i];
+    return scalbn(__ull2double_ru(Q), eall - 30);
 }
 
 struct DepositArgs {
@@ -1453,12 +1590,16 @@ __device__ __forceinline__ void deposit_pairs_col32(const DepositArgs &a, int ax
     }
 }
 
-template <bool TAU, int PREC, bool COUNT>
-__global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
+// MAXT: the block size the kernel is compiled for (launch bound).  The FP32
+// optical-depth deposit has 512-, 768- and 1024-thread builds (128, 80 and 64
+// registers per thread: 16, 24 or 32 warps per SM with the sightline's
+// accumulators on chip); the autotuner picks among them.
+template <bool TAU, int PREC, bool COUNT, int MAXT = (PREC == 0 ? 256 : 512)>
+__global__ void __launch_bounds__(MAXT, 1)
     deposit_kernel(DepositArgs a)
 {
     extern __shared__ __align__(16) unsigned long long smem[];
-    __shared__ double red[32];
+    __shared__ BoundScratch red;
     __shared__ float2 vtab[FSG_V32_N];
     __shared__ int s_bad;
     __shared__ unsigned s_ticket, s_chunk;
@@ -1496,17 +1637,15 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512)
         const int axis = a.t.axis[line];
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
         // 1. fixed-point scale from an upper bound of the sightline total
-        double b = 0.0;
-        for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const double B = order_free_bound(e0, e1, [&](long long e) {
             const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
             if constexpr (TAU && PREC == 1)
-                b += tau_pair_bound32(bk, in);
+                return tau_pair_bound32(bk, in);
             else if constexpr (!TAU && PREC == 1)
-                b += colden_pair_bound32(a.lp, in, btk_abs, col_kfac);
+                return colden_pair_bound32(a.lp, in, btk_abs, col_kfac);
             else
-                b += TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
-        }
-        const double B = block_sum(b, red);
+                return TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
+        }, &red);
         if (threadIdx.x == 0)
             s_bad = !isfinite(B);
         unsigned long long *lo, *hi;
@@ -1721,7 +1860,7 @@ template <int PREC>
 __global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(ChannelArgs a)
 {
     extern __shared__ __align__(16) unsigned long long smem[];
-    __shared__ double red[32];
+    __shared__ BoundScratch red;
     __shared__ int s_bad[MAX_CHANNELS];
     __shared__ double s_B[MAX_CHANNELS];
     __shared__ unsigned s_ticket, s_chunk;
@@ -1744,13 +1883,11 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
         // 1. per-channel bounds, summed exactly as the single-channel deposit sums them
         for (int c = 0; c < nch; c++) {
-            double b = 0.0;
-            for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const double B = order_free_bound(e0, e1, [&](long long e) {
                 const PairInput in = load_pair_ch(a, e, axis, c);
-                b += PREC == 1 ? colden_pair_bound32(a.lp, in, btk_abs, col_kfac)
-                               : colden_pair_bound(a.lp, in, btk);
-            }
-            const double B = block_sum(b, red);
+                return PREC == 1 ? colden_pair_bound32(a.lp, in, btk_abs, col_kfac)
+                                 : colden_pair_bound(a.lp, in, btk);
+            }, &red);
             if (threadIdx.x == 0) {
                 s_B[c] = B;
                 s_bad[c] = !isfinite(B);
@@ -1791,8 +1928,8 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(
                     st.j0 = wrap_bin(col.zlow, nbins);
                     st.kmax = (int)col.kmax;
                     const auto kf = [&](long long z) {
-                        const double plow = btk * (double)z - col.pos1;
-                        return kern_frac<double>(a.lp.kernel, plow, plow + btk, col.smooth,
+                        const double plow = __dsub_rn(__dmul_rn(btk, (double)z), col.pos1);
+                        return kern_frac<double>(a.lp.kernel, plow, __dadd_rn(plow, btk), col.smooth,
                                                  col.dr2, col.zrange);
                     };
                     if constexpr (PREC == 1) {
@@ -1837,8 +1974,9 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(
                     j -= nbins;
                 for (int k = lane; k <= st.kmax; k += 32) {
                     if constexpr (PREC == 0) {
-                        const double plow = btk * (double)(col.zlow + k) - col.pos1;
-                        const double f = kern_frac<double>(a.lp.kernel, plow, plow + btk,
+                        const double plow = __dsub_rn(__dmul_rn(btk, (double)(col.zlow + k)),
+                                                      col.pos1);
+                        const double f = kern_frac<double>(a.lp.kernel, plow, __dadd_rn(plow, btk),
                                                            col.smooth, col.dr2, col.zrange);
 #pragma unroll
                         for (int c = 0; c < MAX_CHANNELS; c++)
@@ -2168,10 +2306,24 @@ __global__ void __launch_bounds__(GRAD_THREADS) grad_kernel(GradArgs a)
 
 int g_max_smem_optin = -1;
 
+// The kernel build for a block size: the FP32 tau form (not counting) has
+// 768- and 1024-thread builds beside the default.
+template <bool TAU, int PREC, bool COUNT>
+decltype(&deposit_kernel<TAU, PREC, COUNT>) deposit_build(int threads)
+{
+    if constexpr (TAU && PREC == 1 && !COUNT) {
+        if (threads > 768)
+            return deposit_kernel<TAU, PREC, COUNT, 1024>;
+        if (threads > 512)
+            return deposit_kernel<TAU, PREC, COUNT, 768>;
+    }
+    return deposit_kernel<TAU, PREC, COUNT>;
+}
+
 template <bool TAU, int PREC, bool COUNT>
 void launch_one(const DepositArgs &a, int grid, int threads, size_t smem, cudaStream_t s)
 {
-    auto k = deposit_kernel<TAU, PREC, COUNT>;
+    auto k = deposit_build<TAU, PREC, COUNT>(threads);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<grid, threads, smem, s>>>(a);
 }
@@ -2179,7 +2331,7 @@ void launch_one(const DepositArgs &a, int grid, int threads, size_t smem, cudaSt
 template <bool TAU, int PREC, bool COUNT>
 int resident_ctas(int threads, size_t smem)
 {
-    auto k = deposit_kernel<TAU, PREC, COUNT>;
+    auto k = deposit_build<TAU, PREC, COUNT>(threads);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem);
@@ -2223,28 +2375,34 @@ void deposit_plan(DepositLaunch &cfg, int compute_tau, int nbins)
 {
     const size_t cap = (size_t)(max_smem_optin() - STATIC_SMEM_RESERVE);
     if (cfg.precision == 1) {
-        // staged pairs per warp: 8 for tau (finer chunks balance the warps
-        // better at the end of a sightline, where pair costs differ most), 32
-        // (or 16 to keep the accumulators on chip) for the column density
-        // far-field tiles (tau) when their node accumulators fit beside the
-        // pixel accumulators, unless switched off
+        // staged pairs per warp (cfg.chunk > 0: as requested): by default 8 for
+        // tau (finer chunks balance the warps better at the end of a
+        // sightline, where pair costs differ most), 32 (or 16 to keep the
+        // accumulators on chip) for the column density; far-field tiles (tau)
+        // when their node accumulators fit beside the pixel accumulators,
+        // unless switched off
         const int first = compute_tau ? 8 : 32;
+        const int asked = cfg.chunk;
         const bool want_tiles = compute_tau && cfg.tiles;
         for (int tiles : {1, 0}) {
             if (tiles && !want_tiles)
                 continue;
             cfg.tiles = tiles;
             for (int chunk : {first, 16, 8}) {
-                if (chunk > first)
+                if (asked > 0)
+                    chunk = asked;
+                else if (chunk > first)
                     continue;
                 cfg.chunk = chunk;
                 cfg.smem_mode = 1;
                 if (deposit_smem_bytes(cfg, compute_tau, nbins) <= cap)
                     return;
+                if (asked > 0)
+                    break;
             }
         }
         cfg.tiles = 0;
-        cfg.chunk = first;
+        cfg.chunk = asked > 0 ? asked : first;
         cfg.smem_mode = 0;
         return;
     }

@@ -73,6 +73,64 @@ __global__ void __launch_bounds__(RED_THREADS) flux_moments_kernel(const double 
     }
 }
 
+// Newton-Raphson on the device (py_module.cpp:242-258): state[0] = the scale
+// of the last pass, state[1] = the next scale, state[2] = 1 once converged,
+// state[3] = passes.  A pass reads the scale from state[1]; once state[2] is
+// set, queued passes and updates return at once, so the host can queue several
+// iterations between reads.
+__global__ void __launch_bounds__(RED_THREADS)
+    flux_moments_dev_kernel(const double *tau, long long n, const double *state, double thresh,
+                            double *part)
+{
+    __shared__ double scratch[RED_THREADS / 32];
+    if (state[2] != 0.0)
+        return;
+    const double scale = state[1];
+    long long lo, hi;
+    block_range(n, lo, hi);
+    double f = 0.0, tf = 0.0, cnt = 0.0;
+    for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
+        const double t = tau[i];
+        if (t > thresh)
+            continue;
+        const double e = exp(-scale * t);
+        f += e;
+        tf += e * t;
+        cnt += 1.0;
+    }
+    f = block_sum_ordered(f, scratch);
+    tf = block_sum_ordered(tf, scratch);
+    cnt = block_sum_ordered(cnt, scratch);
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = f;
+        part[3 * blockIdx.x + 1] = tf;
+        part[3 * blockIdx.x + 2] = cnt;
+    }
+}
+
+// The in-order sums of a pass's block partials and the Newton update (one thread).
+__global__ void newton_update_kernel(const double *part, int nblocks, double mfd, double tol,
+                                     double *state)
+{
+    if (threadIdx.x != 0 || state[2] != 0.0)
+        return;
+    double f = 0.0, tf = 0.0, cnt = 0.0;
+    for (int b = 0; b < nblocks; b++) {
+        f += part[3 * (size_t)b];
+        tf += part[3 * (size_t)b + 1];
+        cnt += part[3 * (size_t)b + 2];
+    }
+    const double scale = state[1];
+    double newscale = scale + (f - mfd * cnt) / tf;
+    if (newscale <= 0)
+        newscale = 1e-10;
+    state[0] = scale;
+    state[1] = newscale;
+    state[3] += 1.0;
+    if (!(fabs(newscale - scale) > tol * newscale))
+        state[2] = 1.0;
+}
+
 // Sum of exp(-scale tau) over all pixels (np.mean(np.exp(-tau)) with scale 1).
 __global__ void __launch_bounds__(RED_THREADS) flux_sum_kernel(const double *tau, long long n,
                                                                double scale, double *part)
@@ -103,32 +161,130 @@ __global__ void partial_sum_kernel(const double *part, int nblocks, int width, d
 // np.histogram with explicit edges (numpy's sorted-search rule): bin j holds
 // e_j <= x < e_{j+1}, the last bin also x == e_last; values outside
 // [e_0, e_last] and NaN are not counted.  x = exp(-scale tau).
-__global__ void flux_hist_kernel(const double *tau, long long n, double scale, const double *edges,
-                                 int nb, unsigned long long *counts)
+//
+// The exponential is taken in FP32 (this GPU runs FP64 at 1/64 of the FP32
+// rate): y = scale tau from float copies of both, x32 = expf(-y).  Relative to
+// the exact exp(-scale tau), x32 is off by at most |y| 2^-21 (the float copies
+// and the product, each within one float ulp, carried through the exponent)
+// plus 2^-21 (expf's 2-ulp bound, doubled for margin), and by at most 2^-148
+// absolutely where it underflows.  A pixel whose x32 is farther than that from
+// every edge lies in the same bin as the FP64 value; the rest (near an edge,
+// outside the bins, NaN) are decided with the FP64 exponential and numpy's
+// comparisons, so the counts equal numpy's.
+//
+// Bins are counted in 32-bit per-warp private histograms in shared memory
+// (nb <= FLUX_WARP_BINS; a warp never counts 2^32 pixels: the grid-stride loop
+// gives each warp at most n / (grid warps) pixels, checked on the host), merged
+// into the 64-bit global counts once per block.  Larger nb: one per-block
+// 64-bit histogram.
+constexpr int FLUX_HIST_THREADS = 256;
+constexpr int FLUX_WARP_BINS = 256;
+
+// float copy of a double by truncating its mantissa (integer operations only;
+// within one float ulp below |d|): 0 for |d| < 2^-126, inf beyond the float range.
+__device__ __forceinline__ float trunc_to_float(double d)
 {
-    extern __shared__ unsigned long long hist[];
-    for (int j = threadIdx.x; j < nb; j += blockDim.x)
-        hist[j] = 0ull;
+    const long long b = __double_as_longlong(d);
+    const unsigned sign = (unsigned)((unsigned long long)b >> 32) & 0x80000000u;
+    const int e11 = (int)((b >> 52) & 0x7ff);
+    if (e11 == 0x7ff)
+        return __int_as_float((int)(sign | 0x7f800000u | (((unsigned)b | (unsigned)(b >> 32)) &
+                                                          0x000fffffu ? 0x400000u : 0u)));
+    const int e8 = e11 - 1023 + 127;
+    if (e8 <= 0)
+        return __int_as_float((int)sign);
+    if (e8 >= 255)
+        return __int_as_float((int)(sign | 0x7f800000u));
+    const unsigned mant = (unsigned)((unsigned long long)b >> 29) & 0x7fffffu;
+    return __int_as_float((int)(sign | ((unsigned)e8 << 23) | mant));
+}
+
+__device__ __forceinline__ int hist_bin64(double x, const double *edges, int nb, double e0,
+                                          double el, double norm)
+{
+    if (!(x >= e0 && x <= el))
+        return -1;
+    int j = (int)((x - e0) * norm);
+    j = j < 0 ? 0 : (j > nb - 1 ? nb - 1 : j);
+    while (j > 0 && x < edges[j])
+        j--;
+    while (j < nb - 1 && x >= edges[j + 1])
+        j++;
+    return j;
+}
+
+template <bool WARP_PRIVATE>
+__global__ void __launch_bounds__(FLUX_HIST_THREADS)
+    flux_hist_kernel(const double *tau, long long n, double scale, const double *edges, int nb,
+                     unsigned long long *counts)
+{
+    // dynamic shared memory: float edges rounded up [nb + 1], rounded down
+    // [nb + 1], then the histograms
+    extern __shared__ __align__(16) unsigned char hraw[];
+    float *eu = reinterpret_cast<float *>(hraw);
+    float *ed = eu + (nb + 1);
+    const size_t eb = ((size_t)2 * (nb + 1) * sizeof(float) + 15) & ~(size_t)15;
+    unsigned *wh_all = reinterpret_cast<unsigned *>(hraw + eb);
+    unsigned long long *bh = reinterpret_cast<unsigned long long *>(hraw + eb);
+    const int warp = threadIdx.x >> 5, nw = FLUX_HIST_THREADS / 32;
+    unsigned *wh = wh_all + (size_t)warp * nb;
+    for (int j = threadIdx.x; j <= nb; j += blockDim.x) {
+        // float bounds of each edge (no FP64 work per pixel): eu >= e >= ed
+        eu[j] = __double2float_ru(edges[j]);
+        ed[j] = __double2float_rd(edges[j]);
+    }
+    if (WARP_PRIVATE) {
+        for (int j = threadIdx.x; j < nb * nw; j += blockDim.x)
+            wh_all[j] = 0u;
+    } else {
+        for (int j = threadIdx.x; j < nb; j += blockDim.x)
+            bh[j] = 0ull;
+    }
     __syncthreads();
     const double e0 = edges[0], el = edges[nb];
     const double norm = nb / (el - e0);
+    const float e0f = (float)e0, normf = (float)norm, vmax = (float)(nb - 1);
+    const float sf = trunc_to_float(scale);
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double x = exp(-scale * tau[i]);
-        if (!(x >= e0 && x <= el))
+        const double t = tau[i];
+        const float y = sf * trunc_to_float(t);
+        const float x32 = expf(-y);
+        const float rel = fmaf(fabsf(y), 4.8e-7f, 4.8e-7f);
+        // exp is never negative: the lower end is clamped at 0
+        const float lo = fmaxf(fmaf(-x32, rel, x32) - 1e-44f, 0.f);
+        const float hi = fmaf(x32, rel, x32) + 1e-44f;
+        // floor of the bin coordinate, clamped, without a float->int conversion
+        // (ties at an integer may land one bin low; the test below then fails)
+        const float v = fminf(fmaxf((x32 - e0f) * normf, 0.f), vmax);
+        int j = __float_as_int(v + (12582912.0f - 0.5f)) - 0x4B400000;
+        j = j < 0 ? 0 : j;
+        // certain: [lo, hi] inside [e_j, e_{j+1}) (the last bin: inside [e_j, e_nb])
+        const bool sure = isfinite(y) && lo >= eu[j] &&
+                          (hi < ed[j + 1] || (j == nb - 1 && hi <= ed[nb]));
+        if (!sure)
+            j = hist_bin64(exp(-scale * t), edges, nb, e0, el, norm);
+        if (j < 0)
             continue;
-        int j = (int)((x - e0) * norm);
-        j = j < 0 ? 0 : (j > nb - 1 ? nb - 1 : j);
-        while (j > 0 && x < edges[j])
-            j--;
-        while (j < nb - 1 && x >= edges[j + 1])
-            j++;
-        atomicAdd(&hist[j], 1ull);
+        if (WARP_PRIVATE)
+            atomicAdd(&wh[j], 1u);
+        else
+            atomicAdd(&bh[j], 1ull);
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < nb; j += blockDim.x)
-        if (hist[j])
-            atomicAdd(&counts[j], hist[j]);
+    if (WARP_PRIVATE) {
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            unsigned long long c = 0;
+            for (int w = 0; w < nw; w++)
+                c += wh_all[(size_t)w * nb + j];
+            if (c)
+                atomicAdd(&counts[j], c);
+        }
+    } else {
+        for (int j = threadIdx.x; j < nb; j += blockDim.x)
+            if (bh[j])
+                atomicAdd(&counts[j], bh[j]);
+    }
 }
 
 // dflux = exp(-scale tau) / mean_flux - 1 for `rows` sightlines.
@@ -165,6 +321,15 @@ void launch_flux_moments(const double *tau, long long n, double scale, double th
     partial_sum_kernel<<<1, 32, 0, s>>>(part, RED_BLOCKS, 3, out3);
 }
 
+void launch_newton_passes(const double *tau, long long n, double mfd, double tol, double thresh,
+                          int passes, double *part, double *state, cudaStream_t s)
+{
+    for (int k = 0; k < passes; k++) {
+        flux_moments_dev_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, state, thresh, part);
+        newton_update_kernel<<<1, 32, 0, s>>>(part, RED_BLOCKS, mfd, tol, state);
+    }
+}
+
 void launch_flux_sum(const double *tau, long long n, double scale, double *part, double *out1,
                      cudaStream_t s)
 {
@@ -174,15 +339,34 @@ void launch_flux_sum(const double *tau, long long n, double scale, double *part,
 
 size_t flux_partials(int width) { return (size_t)RED_BLOCKS * width; }
 
+size_t flux_hist_smem(int nb, bool warp_private)
+{
+    const size_t eb = ((size_t)2 * (nb + 1) * sizeof(float) + 15) & ~(size_t)15;
+    return eb + (warp_private ? sizeof(unsigned) * (size_t)nb * (FLUX_HIST_THREADS / 32)
+                              : sizeof(unsigned long long) * (size_t)nb);
+}
+
 void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
                       unsigned long long *counts, cudaStream_t s)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t smem = sizeof(unsigned long long) * nb;
-    cudaFuncSetAttribute(flux_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    flux_hist_kernel<<<sms * 4, 256, smem, s>>>(tau, n, scale, edges, nb, counts);
+    const int grid = sms * 4;
+    // per-warp 32-bit counters: each warp sees at most ceil(n / (grid threads)) * 32 pixels
+    const long long per_warp = ((n + (long long)grid * FLUX_HIST_THREADS - 1) /
+                                ((long long)grid * FLUX_HIST_THREADS)) * 32;
+    if (nb <= FLUX_WARP_BINS && per_warp < (1ll << 32)) {
+        const size_t smem = flux_hist_smem(nb, true);
+        flux_hist_kernel<true><<<grid, FLUX_HIST_THREADS, smem, s>>>(tau, n, scale, edges, nb,
+                                                                     counts);
+    } else {
+        const size_t smem = flux_hist_smem(nb, false);
+        cudaFuncSetAttribute(flux_hist_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        flux_hist_kernel<false><<<grid, FLUX_HIST_THREADS, smem, s>>>(tau, n, scale, edges, nb,
+                                                                      counts);
+    }
 }
 
 void launch_dflux(const double *tau, long long count, double scale, double inv_mean, double *out,

@@ -209,6 +209,11 @@ void launch_flux_moments(const double *tau, long long n, double scale, double th
                          double *part, double *out3, cudaStream_t s);
 void launch_flux_sum(const double *tau, long long n, double scale, double *part, double *out1,
                      cudaStream_t s);
+// `passes` Newton iterations of the mean-flux scale kept on the device:
+// state[4] = {scale of the last pass, next scale (start: 1), converged, passes},
+// part needs flux_partials(3) doubles.  Passes after convergence do nothing.
+void launch_newton_passes(const double *tau, long long n, double mfd, double tol, double thresh,
+                          int passes, double *part, double *state, cudaStream_t s);
 size_t flux_partials(int width);
 // counts[nb] += np.histogram(exp(-scale tau), edges[nb+1]) (device edges)
 void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
@@ -239,6 +244,7 @@ struct DepositLaunch {
     int smem_mode;           // 1: per-sightline shared-memory accumulators
     int chunk;               // pairs staged per warp (FP32 form), else 0
     int tiles;               // in: allow far-field tiles (FP32 tau); out: planned
+    int tiles_asked;         // what the caller allowed (tiles before planning)
 };
 
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines

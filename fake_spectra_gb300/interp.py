@@ -43,9 +43,11 @@ def _bind_stream(ctx):
 def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, atime, lam, gamma,
                                 fosc, amumass, tautail, pos, vel, dens, temp, h, axis, cofm,
                                 out=None, precision="fp64", threads=0, persistent=-1,
-                                count_work=False, far_tiles=True):
+                                count_work=False, far_tiles=True, chunk=0, tune=0):
     """`_Particle_Interpolate` on device tensors; returns `out` (nlos, nbins) float64 on device.
-    far_tiles=False deposits the far damping wing of the FP32 form pixel by pixel."""
+    far_tiles=False deposits the far damping wing of the FP32 form pixel by pixel.
+    threads/chunk/persistent left at 0/0/-1 take the autotuner's launch in the
+    FP32 form (tune: 0 cached, 1 time again, -1 library defaults)."""
     import torch
     axis, cofm = _host_tables(axis, cofm)
     nlos = int(axis.shape[0])
@@ -58,7 +60,7 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
               _dptr(temp, "float32", "temp") if compute_tau else None,
               _dptr(h, "float32", "h")]
     _bind_stream(ctx)
-    opt = _lib.make_options(precision, threads, persistent, count_work, far_tiles)
+    opt = _lib.make_options(precision, threads, persistent, count_work, far_tiles, chunk, tune)
     eb = _lib.errbuf()
     L = _lib.load()
     rc = L.fsg_particle_interpolate_device(
@@ -72,7 +74,8 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
 
 
 def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, vel, temp, h,
-                         axis, cofm, lines, precision="fp32", threads=0, persistent=-1):
+                         axis, cofm, lines, precision="fp32", threads=0, persistent=-1, chunk=0,
+                         tune=0):
     """Several absorption lines in one call (one sightline search, one CUDA graph).
 
     lines: sequence of (transition, dens, want_tau, want_colden) with
@@ -98,7 +101,7 @@ def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, v
         arr[k].colden = _dptr(col, "float64", "colden") if col is not None else None
         outs.append((tau, col))
     _bind_stream(ctx)
-    opt = _lib.make_options(precision, threads, persistent)
+    opt = _lib.make_options(precision, threads, persistent, chunk=chunk, tune=tune)
     eb = _lib.errbuf()
     L = _lib.load()
     rc = L.fsg_spectra_batch_device(

@@ -40,16 +40,24 @@ typedef enum {
 
 typedef struct {
     int precision;  /* fsg_precision                                         */
-    int threads;    /* threads per deposit CTA; 0 = default                  */
-    int persistent; /* -1 = default, 0 = one CTA per sightline, 1 = resident
-                       CTAs draining a sightline queue                        */
+    int threads;    /* threads per deposit CTA; 0 = tuned (FP32 form) or the
+                       library default                                        */
+    int persistent; /* -1 = tuned (FP32) or default, 0 = one CTA per sightline,
+                       1 = resident CTAs draining a sightline queue           */
     int count_work; /* 1 = run the counting variant of the deposit and report
                        the algorithmic work in fsg_stats (slower; for the
                        roofline only)                                         */
     int no_far_tiles; /* FP32 tau: 1 = deposit the far damping wing pixel by
                        pixel; 0 (default) = through per-tile Chebyshev nodes
                        where the node accumulators fit on chip               */
-    int reserved[3];
+    int chunk;      /* FP32 form: sightline-particle pairs staged per warp
+                       (1..32); 0 = tuned or default                          */
+    int tune;       /* FP32 form, for the launch fields left at 0 / -1 above:
+                       0 = the autotuner's choice for this class of workload,
+                       timed on a sample of the call's sightlines the first
+                       time the class is met, then cached; 1 = time again now;
+                       -1 = library defaults, no tuning                       */
+    int reserved;
 } fsg_options;
 
 typedef struct {
@@ -73,6 +81,18 @@ typedef struct {
     int64_t samples_wing_path;   /* every node asymptotic                  */
     int64_t samples_core_path;   /* every node in the tabulated core       */
     int64_t samples_mixed_path;  /* node by node                           */
+    /* Launch of the last deposit and where it came from */
+    int32_t launch_threads, launch_chunk, launch_persistent;
+    int32_t launch_tuned;        /* 1: from the autotuner (cache or a run in this call) */
+    int32_t tune_ran;            /* 1: the autotuner timed candidates in this call */
+    int32_t tune_candidates;     /* candidates timed by that run */
+    int32_t tune_sample_lines;   /* sightlines of its timing sample */
+    int32_t reserved2;
+    double tune_ms_default;      /* deposit of the sample with the library defaults */
+    double tune_ms_best;         /* ... with the chosen launch */
+    /* host-pointer entry points: the host->device copies of the inputs and the
+     * device->host copy of the output of the last call, device time */
+    double ms_h2d, ms_d2h;
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
@@ -96,6 +116,10 @@ void fsg_context_destroy(fsg_context *ctx);
  * stream here first. */
 int fsg_context_set_stream(fsg_context *ctx, void *cuda_stream);
 int fsg_context_stats(const fsg_context *ctx, fsg_stats *out);
+/* Statistics of the library-owned context of the current device, which the
+ * host-pointer entry points (fsg_particle_interpolate, fsg_near_lines,
+ * fsg_rescale_mean_flux) use; FSG_ERR_VALUE before its first use. */
+int fsg_default_context_stats(fsg_stats *out);
 
 /*
  * Drop-in for _spectra_priv._Particle_Interpolate
@@ -254,6 +278,39 @@ int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box,
  * reference) when sorted != 0, else in arrival order. */
 int fsg_copy_pairs(fsg_context *ctx, int64_t *offsets, int32_t *part, double *dr2, int sorted,
                    char *errbuf, size_t errlen);
+
+/*
+ * Autotuner cache of the FP32 deposit's launch (no counterpart in the
+ * reference, whose only schedule is OpenMP's default over sightlines,
+ * part_int.cpp:25-27).  A workload class is described by fsg_tune_key; its
+ * entry is the launch the tuner chose and the sample timings.  The cache lives
+ * in the process; fsg_tune_cache_file names a text file that it is loaded from
+ * and appended to (also taken from the FSG_TUNE_CACHE environment variable on
+ * first use).  Host-only functions: no GPU is touched.
+ */
+typedef struct {
+    int32_t sms;          /* multiprocessors of the device                       */
+    int32_t precision;    /* fsg_precision                                       */
+    int32_t compute_tau;
+    int32_t kernel;
+    int32_t nbins_b;      /* floor(2 log2 nbins)                                 */
+    int32_t pairs_med_b;  /* floor(2 log2(1 + median pairs per sightline))      */
+    int32_t pairs_p99_b;  /* floor(2 log2(1 + 99th-percentile pairs per line))  */
+    int32_t lines_b;      /* floor(log2 sightlines)                              */
+    int32_t damp_b;       /* floor(2 log2(Gamma lambda / 4 pi / b(T = 1 K)))    */
+} fsg_tune_key;
+
+typedef struct {
+    int32_t threads, chunk, persistent;
+    int32_t candidates, sample_lines;
+    double ms_default, ms_best;
+} fsg_tune_entry;
+
+int fsg_tune_cache_file(const char *path, char *errbuf, size_t errlen);
+int fsg_tune_cache_lookup(const fsg_tune_key *key, fsg_tune_entry *entry); /* 1 found, 0 not */
+int fsg_tune_cache_store(const fsg_tune_key *key, const fsg_tune_entry *entry, char *errbuf,
+                         size_t errlen);
+void fsg_tune_cache_clear(void);   /* empties the in-process cache (the file is kept) */
 
 /*
  * The same interpolation with NO device memory allocation, for callers that

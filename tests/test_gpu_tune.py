@@ -1,0 +1,76 @@
+"""The deposit's launch does not change its output, and the autotuner.
+
+Contributions are added as integers at a scale taken from an order-independent
+bound of each sightline's total, so every launch (threads per block, pairs
+staged per warp, queue mode) gives the same bits; the autotuner may therefore
+pick any of them.  It runs once per workload class and is then served from its
+cache."""
+import numpy as np
+import pytest
+
+from fake_spectra_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(w, ct):
+    import torch
+    a = list(w.call_args(synth.LYA, ct))
+    for k in range(11, 16):
+        a[k] = torch.from_numpy(np.ascontiguousarray(a[k])).cuda()
+    return a
+
+
+@pytest.mark.parametrize("nbins", [111, 3000])
+@pytest.mark.parametrize("compute_tau", [1, 0])
+def test_every_launch_gives_the_same_bits(ctx, compute_tau, nbins):
+    import torch
+    from fake_spectra_gb300 import interp as I
+    w = synth.config0()
+    w.nbins = nbins
+    a = _dev(w, compute_tau)
+    want = I.particle_interpolate_device(ctx, *a, precision="fp32", tune=-1)
+    launches = [(512, 4, 1), (512, 16, 1), (512, 8, 0), (384, 8, 1), (256, 8, 1), (256, 4, 1),
+                (128, 1, 1), (512, 32, 1)]
+    if compute_tau:   # the 768- and 1024-thread builds of the optical-depth kernel
+        launches += [(768, 8, 1), (768, 4, 1), (1024, 4, 1), (1024, 8, 0)]
+    for threads, chunk, persistent in launches:
+        got = I.particle_interpolate_device(ctx, *a, precision="fp32", threads=threads,
+                                            chunk=chunk, persistent=persistent)
+        assert torch.equal(got, want), (threads, chunk, persistent)
+    w64 = I.particle_interpolate_device(ctx, *a, precision="fp64")
+    for threads, persistent in [(128, 0), (256, 1), (64, 1)]:
+        got = I.particle_interpolate_device(ctx, *a, precision="fp64", threads=threads,
+                                            persistent=persistent)
+        assert torch.equal(got, w64), (threads, persistent)
+
+
+def test_tuner_runs_once_per_class_and_keeps_the_bits(ctx):
+    import torch
+    from fake_spectra_gb300 import _lib, interp as I
+    _lib.tune_cache_clear()
+    w = synth.config0()
+    w.nbins = 3000
+    a = _dev(w, 1)
+    want = I.particle_interpolate_device(ctx, *a, precision="fp32", tune=-1)
+    st = ctx.stats()
+    assert not st["launch"]["tuned"] and not st["tune"]["ran"]
+    first = I.particle_interpolate_device(ctx, *a, precision="fp32")
+    st = ctx.stats()
+    assert st["launch"]["tuned"] and st["tune"]["ran"]
+    assert st["tune"]["candidates"] >= 1 and st["tune"]["sample_lines"] == w.nlos
+    assert st["tune"]["ms_best"] <= st["tune"]["ms_default"]
+    second = I.particle_interpolate_device(ctx, *a, precision="fp32")
+    st2 = ctx.stats()
+    assert st2["launch"]["tuned"] and not st2["tune"]["ran"]
+    assert st2["launch"] == st["launch"]
+    assert torch.equal(first, want) and torch.equal(second, want)
+    # tune=1 times the candidates again; the batched entry uses the same tuner
+    I.particle_interpolate_device(ctx, *a, precision="fp32", tune=1)
+    assert ctx.stats()["tune"]["ran"]
+    (tau, col), = I.spectra_batch_device(ctx, w.nbins, w.kernel, w.box, w.velfac, w.atime,
+                                         w.tautail, a[11], a[12], a[14], a[15], w.axis, w.cofm,
+                                         [(synth.LYA, a[13], True, True)])
+    assert torch.equal(tau, want)
+    cw = I.particle_interpolate_device(ctx, *_dev(w, 0), precision="fp32", tune=-1)
+    assert torch.equal(col, cw)
