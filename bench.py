@@ -616,8 +616,8 @@ def main():
                 "order, about four per resident block; all give the same output bits"}
     if args.sweep:
         sweep = {}
-        for th, ch, pm in ((512, 8, 1), (512, 4, 1), (512, 16, 1), (512, 8, 0), (768, 8, 1),
-                           (768, 4, 1), (1024, 4, 1), (1024, 8, 1)):
+        for th, ch, pm in ((512, 8, 1), (512, 16, 1), (768, 8, 1), (1024, 8, 1), (1024, 4, 1),
+                           (1024, 8, 0)):
             ms = []
             for _ in range(2):
                 step("fp32", threads=th, chunk=ch, persistent=pm)
@@ -656,6 +656,7 @@ def main():
         for _ in range(ke):
             c_call()
         dt = allreduce_max((time.perf_counter() - t0) / ke, world)
+        dst = _lib.default_context_stats() or {}
         # (b) the Python drop-in: a new zeroed array per call, as the reference
         # returns, so each call also pays the first touch and the release of
         # 2.9 GB of host pages
@@ -666,7 +667,7 @@ def main():
             tau_d = _Particle_Interpolate(*hargs, precision="fp32")
         dt_d = allreduce_max((time.perf_counter() - t0) / ke, world)
         e2e_clk = ck.stop()
-        dst = _lib.default_context_stats() or {}
+        dst_d = _lib.default_context_stats() or {}
         same = bool(np.array_equal(tau_d, tau_h))
         del tau_d
         res["e2e"] = {"value": world * pixels / dt, "unit": "pixels/s",
@@ -678,6 +679,9 @@ def main():
                       "api": "fsg_particle_interpolate (host pointers; inputs pinned, output a "
                              "pageable array the caller allocated once)",
                       "dropin": {"value": world * pixels / dt_d, "ms_per_step": dt_d * 1e3,
+                                 "phases_ms_last_call": {
+                                     k: dst_d.get(k) for k in ("ms_h2d", "ms_search",
+                                                               "ms_deposit", "ms_d2h")},
                                  "api": "_spectra_priv._Particle_Interpolate (new output "
                                         "array per call)",
                                  "same_result": same},

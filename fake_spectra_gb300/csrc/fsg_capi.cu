@@ -88,6 +88,11 @@ struct fsg_context {
     DevBuf tune_order;                                       // autotuner sample
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t cp[2] = {nullptr, nullptr};   // copy timing of the host-pointer entries
+    // host-pointer entries: the inputs the search does not read are uploaded on
+    // `side` while the search runs; up[0] orders them after the search's
+    // inputs, up[1] orders the deposit after them
+    cudaStream_t side = nullptr;
+    cudaEvent_t up[2] = {nullptr, nullptr};
     // host mirrors
     std::vector<long long> h_off;
     std::vector<int> h_order;
@@ -662,7 +667,7 @@ fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particle
     std::vector<Cand> cands;
     if (lp.compute_tau)
         cands = {{512, 8, 1}, {512, 4, 1}, {512, 16, 1}, {512, 8, 0}, {256, 8, 1},
-                 {768, 8, 1}, {768, 4, 1}, {1024, 4, 1}, {1024, 8, 1}};
+                 {768, 8, 1}, {768, 16, 1}, {1024, 4, 1}, {1024, 8, 1}, {1024, 16, 1}};
     else
         cands = {{512, 32, 1}, {512, 16, 1}, {512, 8, 1}, {512, 32, 0}, {256, 32, 1},
                  {256, 16, 1}};
@@ -887,6 +892,9 @@ void ctx_init(fsg_context *c, int device)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
     for (auto &e : c->cp)
         cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    cuda_check(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (auto &e : c->up)
+        cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 }
 
 // Writes zeros over a caller's host output from a few threads while the GPU
@@ -1019,11 +1027,15 @@ const float2 *voronoi_cells(fsg_context *c, const Particles &p, const double *co
 void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, double box,
                      double velfac, double lambda, double gamma, double fosc, double amumass,
                      double tautail, const Particles &p, const int32_t *axis, const double *cofm,
-                     int32_t nlos, double *out, const fsg_options *opt)
+                     int32_t nlos, double *out, const fsg_options *opt,
+                     cudaEvent_t inputs_ready = nullptr)
 {
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
     build_tables(c, axis, cofm, nlos, box);
     search_pairs(c, p, nlos);
+    // the inputs only the deposit reads may still be on their way (host-pointer entry)
+    if (inputs_ready)
+        cuda_check(cudaStreamWaitEvent(c->stream, inputs_ready, 0), "wait for uploads");
     LineParams lp = make_line_params(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
                                      amumass, tautail);
     const float2 *seg = kernel == VORONOI ? voronoi_cells(c, p, cofm, box) : nullptr;
@@ -1088,6 +1100,13 @@ void fsg_context_destroy(fsg_context *ctx)
     for (auto &e : ctx->cp)
         if (e)
             cudaEventDestroy(e);
+    for (auto &e : ctx->up)
+        if (e)
+            cudaEventDestroy(e);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
     if (ctx->graph)
         cudaGraphExecDestroy(ctx->graph);
     if (ctx->own)
@@ -1170,23 +1189,44 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
                 cuda_check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s), "H2D");
             return (const float *)d;
         };
+        // no copy of the caller's arrays may outlive the call, error returns included
+        struct SideSync {
+            fsg_context *c;
+            ~SideSync()
+            {
+                cudaStreamSynchronize(c->side);
+                cudaStreamSynchronize(c->stream);
+            }
+        } side_sync{c};
         Particles p;
         p.n = npart;
+        // the search reads pos and h: they go first; vel, dens and temp follow on
+        // the side stream while the search runs (the deposit waits for them)
         cuda_check(cudaEventRecord(c->cp[0], s), "event");
         p.pos = up(c->pos, pos, n3);
-        p.dens = up(c->dens, dens, n1);
         p.hh = up(c->hh, h, n1);
-        p.vel = compute_tau ? up(c->vel, vel, n3) : nullptr;
-        p.temp = compute_tau ? up(c->temp, temp, n1) : nullptr;
-        cuda_check(cudaEventRecord(c->cp[1], s), "event");
+        cuda_check(cudaEventRecord(c->up[0], s), "event");
+        cuda_check(cudaStreamWaitEvent(c->side, c->up[0], 0), "order uploads");
+        const auto up_side = [&](DevBuf &b, const void *src, size_t bytes) -> const float * {
+            void *d = c->ensure(b, bytes);
+            if (bytes)
+                cuda_check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, c->side),
+                           "H2D");
+            return (const float *)d;
+        };
+        p.dens = up_side(c->dens, dens, n1);
+        p.vel = compute_tau ? up_side(c->vel, vel, n3) : nullptr;
+        p.temp = compute_tau ? up_side(c->temp, temp, n1) : nullptr;
+        cuda_check(cudaEventRecord(c->up[1], c->side), "event");
+        cuda_check(cudaEventRecord(c->cp[1], c->side), "event");
         const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
         double *dout = (double *)c->ensure(c->out, nout);
         PreTouch touch(out, nout);
         run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
-                        tautail, p, axis, cofm, nlos, dout, opt);
+                        tautail, p, axis, cofm, nlos, dout, opt, c->up[1]);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
-        c->stats.ms_h2d = ms;
+        c->stats.ms_h2d = ms;   // from the first upload to the last (search overlapped)
         touch.wait();
         cuda_check(cudaEventRecord(c->cp[0], s), "event");
         if (nout)
