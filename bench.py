@@ -105,6 +105,9 @@ def parse_args():
                    help="skip the 256^3 cubic-spline / top-hat section")
     p.add_argument("--sweep", action="store_true",
                    help="time every launch candidate on the full call (autotuner evidence)")
+    p.add_argument("--launch", default="",
+                   help="threads,chunk,persistent[,records] of the FP32 deposit instead of the "
+                        "autotuner's choice (no tuning run; for profiling a fixed launch)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
@@ -516,11 +519,17 @@ def main():
 
     # ---- the autotuner picks the FP32 deposit's launch (timed on a sample of the
     # call's sightlines), untimed; the calls below use its cached choice
-    step("fp32", tune=1)
+    fixed = {}
+    if args.launch:
+        v = [int(x) for x in args.launch.split(",")]
+        fixed = dict(threads=v[0], chunk=v[1], persistent=v[2],
+                     records=v[3] if len(v) > 3 else 0)
+    else:
+        step("fp32", tune=1)
     tuned = ctx.stats()
     # ---- tuned FP32 form: the timed region
     for _ in range(args.warmup):
-        step("fp32")
+        step("fp32", **fixed)
     stream = torch.cuda.current_stream()
     launches0 = ctx.stats()["gpu_launches"]
     clocks = ClockSampler(local).start()
@@ -530,7 +539,7 @@ def main():
     ev0.record(stream)
     dep_ms, search_ms = [], []
     for _ in range(args.steps):
-        step("fp32")
+        step("fp32", **fixed)
         st = ctx.stats()
         dep_ms.append(st["ms_deposit"])
         search_ms.append(st["ms_search"])
@@ -616,13 +625,14 @@ def main():
                 "order, about four per resident block; all give the same output bits"}
     if args.sweep:
         sweep = {}
-        for th, ch, pm in ((512, 8, 1), (512, 16, 1), (768, 8, 1), (1024, 8, 1), (1024, 4, 1),
-                           (1024, 8, 0)):
+        for th, ch, pm, rc in ((512, 8, 1, 0), (512, 16, 1, 0), (768, 8, 1, 0), (1024, 8, 1, 0),
+                               (1024, 4, 1, 0), (1024, 8, 0, 0), (1024, 8, 1, 1),
+                               (768, 8, 1, 1)):
             ms = []
             for _ in range(2):
-                step("fp32", threads=th, chunk=ch, persistent=pm)
+                step("fp32", threads=th, chunk=ch, persistent=pm, records=rc)
                 ms.append(ctx.stats()["ms_deposit"])
-            sweep["%d_%d_%d" % (th, ch, pm)] = min(ms)
+            sweep["%d_%d_%d%s" % (th, ch, pm, "_records" if rc else "")] = min(ms)
         res["autotune"]["full_call_sweep_ms"] = sweep
 
     # ---- end to end through the host-pointer C ABI (copies inside the timed region),

@@ -62,7 +62,7 @@ _c_size = ctypes.c_size_t
 class Options(ctypes.Structure):
     _fields_ = [("precision", _c_int), ("threads", _c_int), ("persistent", _c_int),
                 ("count_work", _c_int), ("no_far_tiles", _c_int), ("chunk", _c_int),
-                ("tune", _c_int), ("reserved", _c_int)]
+                ("tune", _c_int), ("records", _c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -74,7 +74,7 @@ class Stats(ctypes.Structure):
                 ("samples_mixed_path", _c_i64), ("launch_threads", _c_i32),
                 ("launch_chunk", _c_i32), ("launch_persistent", _c_i32),
                 ("launch_tuned", _c_i32), ("tune_ran", _c_i32), ("tune_candidates", _c_i32),
-                ("tune_sample_lines", _c_i32), ("reserved2", _c_i32),
+                ("tune_sample_lines", _c_i32), ("launch_records", _c_i32),
                 ("tune_ms_default", _c_d), ("tune_ms_best", _c_d), ("ms_h2d", _c_d),
                 ("ms_d2h", _c_d)]
 
@@ -86,8 +86,8 @@ class TuneKey(ctypes.Structure):
 
 class TuneEntry(ctypes.Structure):
     _fields_ = [("threads", _c_i32), ("chunk", _c_i32), ("persistent", _c_i32),
-                ("candidates", _c_i32), ("sample_lines", _c_i32), ("ms_default", _c_d),
-                ("ms_best", _c_d)]
+                ("records", _c_i32), ("candidates", _c_i32), ("sample_lines", _c_i32),
+                ("ms_default", _c_d), ("ms_best", _c_d)]
 
 
 class Line(ctypes.Structure):
@@ -193,12 +193,13 @@ def errbuf():
 
 
 def make_options(precision="fp64", threads=0, persistent=-1, count_work=False, far_tiles=True,
-                 chunk=0, tune=0):
-    """fsg_options.  threads/chunk 0 and persistent -1 leave the launch to the
-    autotuner (FP32 form; tune 0 = cached choice, 1 = time again, -1 = library
-    defaults) or to the library defaults (FP64 form)."""
+                 chunk=0, tune=0, records=-1):
+    """fsg_options.  threads/chunk 0 and persistent/records -1 leave the launch to
+    the autotuner (FP32 form; tune 0 = cached choice, 1 = time again, -1 =
+    library defaults) or to the library defaults (FP64 form)."""
     o = Options()
     o.chunk = int(chunk)
+    o.records = int(records)
     o.tune = int(tune)
     o.count_work = int(bool(count_work))
     o.no_far_tiles = int(not far_tiles)
@@ -271,7 +272,7 @@ def _stats_dict(s):
             "samples_mixed_path": int(s.samples_mixed_path),
             "launch": {"threads": int(s.launch_threads), "chunk": int(s.launch_chunk),
                        "persistent": int(s.launch_persistent),
-                       "tuned": bool(s.launch_tuned)},
+                       "records": int(s.launch_records), "tuned": bool(s.launch_tuned)},
             "tune": {"ran": bool(s.tune_ran), "candidates": int(s.tune_candidates),
                      "sample_lines": int(s.tune_sample_lines),
                      "ms_default": float(s.tune_ms_default),
@@ -307,8 +308,9 @@ def tune_cache_lookup(key):
 
 
 def tune_cache_store(key, threads, chunk, persistent, ms_default=0.0, ms_best=0.0,
-                     candidates=0, sample_lines=0):
-    e = TuneEntry(threads, chunk, persistent, candidates, sample_lines, ms_default, ms_best)
+                     candidates=0, sample_lines=0, records=0):
+    e = TuneEntry(threads, chunk, persistent, records, candidates, sample_lines, ms_default,
+                  ms_best)
     eb = errbuf()
     raise_for(load().fsg_tune_cache_store(ctypes.byref(key), ctypes.byref(e), eb, 512),
               eb.value.decode())

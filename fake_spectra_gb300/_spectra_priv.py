@@ -87,7 +87,8 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1, chunk=0, tune=0):
+def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1, chunk=0, tune=0,
+                          records=-1):
     """tau or colden along every sightline; see the module docstring.  The keyword
     arguments select the form (precision) and the deposit launch (FP32 form:
     left at 0/-1 the autotuner picks it)."""
@@ -111,7 +112,8 @@ def _Particle_Interpolate(*args, precision="fp64", threads=0, persistent=-1, chu
     if nlos == 0 or nbins == 0:
         return out
     L = _lib.load()
-    opt = _lib.make_options(precision, threads, persistent, chunk=chunk, tune=tune)
+    opt = _lib.make_options(precision, threads, persistent, chunk=chunk, tune=tune,
+                            records=records)
     eb = _lib.errbuf()
     rc = L.fsg_particle_interpolate(int(compute_tau), nbins, kernel, box, velfac, atime, lam,
                                     gamma, fosc, amumass, tautail, _ptr(pos),

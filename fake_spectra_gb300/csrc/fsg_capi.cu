@@ -86,6 +86,7 @@ struct fsg_context {
     DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
     DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
     DevBuf tune_order;                                       // autotuner sample
+    DevBuf prec;                                             // pair records (FP32 tau)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t cp[2] = {nullptr, nullptr};   // copy timing of the host-pointer entries
     // host-pointer entries: the inputs the search does not read are uploaded on
@@ -128,7 +129,7 @@ struct fsg_context {
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
-                          &ffft, &fpower, &vseg, &vscratch, &vcofm, &tune_order};
+                          &ffft, &fpower, &vseg, &vscratch, &vcofm, &tune_order, &prec};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -395,7 +396,7 @@ double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale
 
 DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_options *opt);
 void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, const Particles &p,
-                  const PairLists &pl, double *out, DepositLaunch &cfg);
+                  PairLists pl, double *out, DepositLaunch &cfg);
 
 // 3. deposit into out (device, nlos*nbins)
 void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
@@ -418,6 +419,8 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
     DepositLaunch cfg = deposit_config(c, lp, opt);
     // the tuner times candidates on sample rows of `out`, which is cleared below
     apply_tuning(c, lp, opt, p, pl, out, cfg);
+    if (cfg.rec)
+        pl.rec = c->ensure(c->prec, 32 * (size_t)c->npairs);
     cuda_check(cudaEventRecord(c->ev[2], s), "event");
     cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * nout, s), "memset out");
     unsigned long long *gacc = nullptr;
@@ -509,9 +512,15 @@ DepositLaunch deposit_config(fsg_context *c, const LineParams &lp, const fsg_opt
     const bool vor = lp.kernel == VORONOI;
     if (vor)
         cfg.precision = FSG_PREC_FP64;
-    // FP32 optical depths have 768- and 1024-thread kernel builds
+    // FP32 optical depths have 768- and 1024-thread kernel builds and may go
+    // through pair records (the context's buffer); the counting variant has not
+    const bool count = opt && opt->count_work;
+    const bool tau32 = cfg.precision == FSG_PREC_FP32 && lp.compute_tau && !vor && !count;
+    cfg.rec = tau32 && opt && opt->records == 1;
+    if (opt && opt->records > 1)
+        fail(FSG_ERR_VALUE, "records must be -1 (tuned), 0 or 1");
     const int tdef = cfg.precision == FSG_PREC_FP64 ? 256 : 512;
-    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : (lp.compute_tau ? 1024 : 512);
+    const int tmax = cfg.precision == FSG_PREC_FP64 ? 256 : (tau32 ? 1024 : 512);
     cfg.threads = (opt && opt->threads > 0 && !vor) ? opt->threads : tdef;
     if (cfg.threads % 32 || cfg.threads > tmax)
         fail(FSG_ERR_VALUE, "threads must be a multiple of 32 and at most %d", tmax);
@@ -550,7 +559,14 @@ std::map<fsg_tune_key, fsg_tune_entry, TuneKeyLess> g_tune;
 std::string g_tune_file;
 bool g_tune_env_read = false;
 
-constexpr const char *TUNE_FILE_TAG = "fsg-tune-v1";
+constexpr const char *TUNE_FILE_TAG = "fsg-tune-v2";
+
+bool tune_entry_valid(const fsg_tune_entry &e)
+{
+    return e.threads > 0 && e.threads % 32 == 0 && e.threads <= 1024 && e.chunk >= 1 &&
+           e.chunk <= 32 && (e.persistent == 0 || e.persistent == 1) &&
+           (e.records == 0 || e.records == 1);
+}
 
 // Reads the entries of a cache file (lines that do not parse are skipped);
 // the caller holds g_tune_mu.
@@ -564,13 +580,12 @@ void tune_load_locked(const std::string &path)
         char tag[32];
         fsg_tune_key k{};
         fsg_tune_entry e{};
-        const int n = sscanf(line, "%31s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %lf %lf", tag,
-                             &k.sms, &k.precision, &k.compute_tau, &k.kernel, &k.nbins_b,
+        const int n = sscanf(line, "%31s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %lf %lf",
+                             tag, &k.sms, &k.precision, &k.compute_tau, &k.kernel, &k.nbins_b,
                              &k.pairs_med_b, &k.pairs_p99_b, &k.lines_b, &k.damp_b, &e.threads,
-                             &e.chunk, &e.persistent, &e.candidates, &e.sample_lines,
+                             &e.chunk, &e.persistent, &e.records, &e.candidates, &e.sample_lines,
                              &e.ms_default, &e.ms_best);
-        if (n == 17 && strcmp(tag, TUNE_FILE_TAG) == 0 && e.threads > 0 && e.threads % 32 == 0 &&
-            e.chunk >= 1 && e.chunk <= 32 && (e.persistent == 0 || e.persistent == 1))
+        if (n == 18 && strcmp(tag, TUNE_FILE_TAG) == 0 && tune_entry_valid(e))
             g_tune[k] = e;
     }
     fclose(f);
@@ -596,10 +611,10 @@ bool tune_store_locked(const fsg_tune_key &k, const fsg_tune_entry &e)
     FILE *f = fopen(g_tune_file.c_str(), "a");
     if (!f)
         return false;
-    fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %.6f %.6f\n", TUNE_FILE_TAG, k.sms,
-            k.precision, k.compute_tau, k.kernel, k.nbins_b, k.pairs_med_b, k.pairs_p99_b,
-            k.lines_b, k.damp_b, e.threads, e.chunk, e.persistent, e.candidates, e.sample_lines,
-            e.ms_default, e.ms_best);
+    fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %d %d %d %d %d %.6f %.6f\n", TUNE_FILE_TAG,
+            k.sms, k.precision, k.compute_tau, k.kernel, k.nbins_b, k.pairs_med_b, k.pairs_p99_b,
+            k.lines_b, k.damp_b, e.threads, e.chunk, e.persistent, e.records, e.candidates,
+            e.sample_lines, e.ms_default, e.ms_best);
     fclose(f);
     return true;
 }
@@ -641,7 +656,7 @@ void finish_config(fsg_context *c, const LineParams &lp, DepositLaunch &cfg)
 // CTA so that the queue's balance resembles the full call's) and returns the
 // fastest.  The sample rows of `out` are overwritten.
 fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particles &p,
-                            const PairLists &pl, double *out, const DepositLaunch &base)
+                            PairLists pl, double *out, const DepositLaunch &base)
 {
     cudaStream_t s = c->stream;
     const int nlos = c->nlos;
@@ -662,15 +677,16 @@ fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particle
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 *
                                                             (size_t)nlos * lp.nbins);
     struct Cand {
-        int threads, chunk, persistent;
+        int threads, chunk, persistent, rec;
     };
     std::vector<Cand> cands;
     if (lp.compute_tau)
-        cands = {{512, 8, 1}, {512, 4, 1}, {512, 16, 1}, {512, 8, 0}, {256, 8, 1},
-                 {768, 8, 1}, {768, 16, 1}, {1024, 4, 1}, {1024, 8, 1}, {1024, 16, 1}};
+        cands = {{512, 8, 1, 0},  {512, 4, 1, 0},  {512, 16, 1, 0},  {512, 8, 0, 0},
+                 {256, 8, 1, 0},  {768, 8, 1, 0},  {768, 16, 1, 0},  {1024, 4, 1, 0},
+                 {1024, 8, 1, 0}, {1024, 16, 1, 0}, {1024, 8, 1, 1}, {768, 8, 1, 1}};
     else
-        cands = {{512, 32, 1}, {512, 16, 1}, {512, 8, 1}, {512, 32, 0}, {256, 32, 1},
-                 {256, 16, 1}};
+        cands = {{512, 32, 1, 0}, {512, 16, 1, 0}, {512, 8, 1, 0}, {512, 32, 0, 0},
+                 {256, 32, 1, 0}, {256, 16, 1, 0}};
     fsg_tune_entry best{};
     best.ms_best = 1e300;
     best.sample_lines = nsamp;
@@ -679,6 +695,7 @@ fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particle
         cfg.threads = cd.threads;
         cfg.chunk = cd.chunk;
         cfg.persistent = cd.persistent;
+        cfg.rec = cd.rec;
         cfg.tiles = base.tiles_asked;
         deposit_plan(cfg, lp.compute_tau, lp.nbins);
         if (cfg.smem_mode != base.smem_mode || cfg.tiles != base.tiles)
@@ -687,6 +704,7 @@ fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particle
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
         const int per_sm = std::max(1, deposit_resident_ctas(cfg, lp.compute_tau, lp.nbins));
         cfg.grid = std::min(nsamp, sms * per_sm);
+        pl.rec = cfg.rec ? c->ensure(c->prec, 32 * (size_t)c->npairs) : nullptr;
         float ms_min = 1e30f;
         for (int rep = 0; rep < 2; rep++) {
             cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
@@ -704,35 +722,38 @@ fsg_tune_entry tune_deposit(fsg_context *c, const LineParams &lp, const Particle
         }
         best.candidates++;
         if (cd.threads == base.threads && cd.chunk == base.chunk &&
-            cd.persistent == base.persistent)
+            cd.persistent == base.persistent && cd.rec == base.rec)
             best.ms_default = ms_min;
         if (ms_min < best.ms_best) {
             best.ms_best = ms_min;
             best.threads = cd.threads;
             best.chunk = cd.chunk;
             best.persistent = cd.persistent;
+            best.records = cd.rec;
         }
     }
     if (best.candidates == 0) {   // nothing kept the layout: the defaults
         best.threads = base.threads;
         best.chunk = base.chunk;
         best.persistent = base.persistent;
+        best.records = base.rec;
         best.ms_best = best.ms_default = 0.0;
     }
     return best;
 }
 
 void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, const Particles &p,
-                  const PairLists &pl, double *out, DepositLaunch &cfg)
+                  PairLists pl, double *out, DepositLaunch &cfg)
 {
     c->stats.launch_threads = cfg.threads;
     c->stats.launch_chunk = cfg.chunk;
     c->stats.launch_persistent = cfg.persistent;
+    c->stats.launch_records = cfg.rec;
     c->stats.launch_tuned = 0;
     const int mode = opt ? opt->tune : 0;
     if (cfg.precision != FSG_PREC_FP32 || lp.kernel == VORONOI || mode < 0 || !opt ||
         opt->count_work || opt->threads > 0 || opt->chunk > 0 || opt->persistent >= 0 ||
-        c->nlos <= 0 || pl.seg)
+        opt->records >= 0 || c->nlos <= 0 || pl.seg)
         return;
     const fsg_tune_key key = tune_key(c, lp, cfg.precision);
     fsg_tune_entry e{};
@@ -760,6 +781,7 @@ void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, 
     t.threads = e.threads;
     t.chunk = e.chunk;
     t.persistent = e.persistent;
+    t.rec = lp.compute_tau ? e.records : 0;
     t.tiles = cfg.tiles_asked;
     deposit_plan(t, lp.compute_tau, lp.nbins);
     if (t.smem_mode != cfg.smem_mode || t.tiles != cfg.tiles)
@@ -769,6 +791,7 @@ void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, 
     c->stats.launch_threads = cfg.threads;
     c->stats.launch_chunk = cfg.chunk;
     c->stats.launch_persistent = cfg.persistent;
+    c->stats.launch_records = cfg.rec;
     c->stats.launch_tuned = 1;
 }
 
@@ -791,6 +814,9 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
         p.dens = dens[k];
         apply_tuning(c, lps[k], opt, p, pl, outs[k], cfgs.back());
     }
+    for (const DepositLaunch &cf : cfgs)
+        if (cf.rec)
+            pl.rec = c->ensure(c->prec, 32 * (size_t)c->npairs);
     unsigned long long *gacc = nullptr;
     if (!cfgs[0].smem_mode)
         gacc = (unsigned long long *)c->ensure(c->gacc, sizeof(unsigned long long) * 2 * nout);
@@ -808,6 +834,7 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
     putp(c->part.p);
     putp(c->dr2.p);
     putp(c->line_order.p);
+    putp(pl.rec);
     putp(c->key.p);
     putp(c->second.p);
     putp(c->axis.p);
@@ -835,6 +862,7 @@ void run_batch(fsg_context *c, const std::vector<LineParams> &lps,
         put(cfgs[k].grid);
         put(cfgs[k].chunk);
         put(cfgs[k].tiles);
+        put(cfgs[k].rec);
     }
     cudaStream_t s = c->own;
     cuda_check(cudaStreamSynchronize(c->stream), "sync caller stream");
@@ -1695,11 +1723,9 @@ int fsg_tune_cache_store(const fsg_tune_key *key, const fsg_tune_entry *entry, c
     try {
         if (!key || !entry)
             fail(FSG_ERR_VALUE, "key and entry must not be NULL");
-        if (entry->threads <= 0 || entry->threads % 32 || entry->threads > 1024 ||
-            entry->chunk < 1 || entry->chunk > 32 ||
-            (entry->persistent != 0 && entry->persistent != 1))
+        if (!tune_entry_valid(*entry))
             fail(FSG_ERR_VALUE, "not a valid launch: threads a multiple of 32 up to 1024, "
-                                "chunk 1..32, persistent 0 or 1");
+                                "chunk 1..32, persistent and records 0 or 1");
         std::lock_guard<std::mutex> lock(g_tune_mu);
         tune_env_locked();
         if (!tune_store_locked(*key, *entry))

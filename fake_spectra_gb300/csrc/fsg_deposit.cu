@@ -439,6 +439,111 @@ __device__ __forceinline__ PairInput load_pair(const Particles &p, const PairLis
     return in;
 }
 
+// ------------------------------------------------------ staged pair records
+// The FP32 optical-depth deposit reads each pair's particle fields three
+// times (two bound passes and the chunk staging).  The first bound pass
+// gathers them from the particle arrays once and writes a 32-byte record per
+// pair, contiguous in pair order; the second pass reads the records, and each
+// warp stages a chunk's records into shared memory with one bulk asynchronous
+// copy (cp.async.bulk, completion on an mbarrier) instead of seven scattered
+// loads per pair.
+struct __align__(16) PairRec {
+    float ppos, pvel, temp, smooth;
+    float dens;
+    int part;
+    double dr2;
+};
+static_assert(sizeof(PairRec) == 32, "PairRec is two 16-byte words");
+
+__device__ __forceinline__ PairRec make_rec(const PairInput &in, int part)
+{
+    PairRec r;
+    r.ppos = in.ppos;
+    r.pvel = in.pvel;
+    r.temp = in.temp;
+    r.smooth = in.smooth;
+    r.dens = in.dens;
+    r.part = part;
+    r.dr2 = in.dr2;
+    return r;
+}
+
+__device__ __forceinline__ PairInput rec_input(const PairRec &r)
+{
+    PairInput in;
+    in.dr2 = r.dr2;
+    in.dens = r.dens;
+    in.ppos = r.ppos;
+    in.pvel = r.pvel;
+    in.temp = r.temp;
+    in.smooth = r.smooth;
+    return in;
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Orders this thread's earlier generic-proxy accesses (to global, or to
+// shared memory) before later async-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One elected thread: expect `bytes` on the barrier and start the copy of
+// `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to
+// shared memory; the barrier's phase completes when they have landed.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes,
+                                              unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Waits for the barrier phase with parity `parity`; gives up after `tries`
+// polls (each poll may suspend the thread for a while) and returns false.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int tries)
+{
+    const unsigned a = smem_addr(bar);
+    for (int i = 0; i < tries; i++) {
+        unsigned done = 0;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+constexpr int STAGE_WAIT_TRIES = 1 << 20;
+
+// Per warp of a deposit block: the barrier of its staged record copies and the
+// parity of the phase it waits for next (kept here rather than in registers,
+// which the pixel walk needs).
+__shared__ unsigned long long s_stage_bar[32];
+__shared__ unsigned s_stage_phase[32];
+
 // Work counters of the counting variant (per lane, reduced per CTA at exit):
 // a core-branch evals, b wing-branch evals, c other evals, pixels, and d the
 // wing evals among b that were summed through the multipole form.
@@ -1083,15 +1188,17 @@ __device__ __forceinline__ double colden_pair_bound32(const LineParams &lp, cons
 // The fixed-point scale follows from ilogb(B), so the output bits are the same
 // for every block size, chunk size and queue mode.  Returns +inf when a bound
 // is not finite (the sightline then goes to the non-finite fallback) and 0 when
-// every bound is 0.  `bound(e)` is evaluated twice per pair.
+// every bound is 0.  `bound(e)` is evaluated in the first pass and
+// `bound_again(e)` (the same value, possibly from a cheaper source) in the
+// second; each pair is visited by the same thread in both.
 struct BoundScratch {
     int em[32];
     unsigned long long q[32];
 };
 
-template <class BoundFn>
+template <class BoundFn, class AgainFn>
 __device__ __forceinline__ double order_free_bound(long long e0, long long e1, BoundFn bound,
-                                                   BoundScratch *sc)
+                                                   AgainFn bound_again, BoundScratch *sc)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int NONE = -2147483647;
@@ -1121,7 +1228,7 @@ __device__ __forceinline__ double order_free_bound(long long e0, long long e1, B
         return 0.0;
     unsigned long long q = 0;
     for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const double b = bound(e);
+        const double b = bound_again(e);
         if (b > 0.0)
             q += (unsigned long long)ceil(scalbn(b, 30 - eall));
     }
@@ -1480,7 +1587,7 @@ __device__ __forceinline__ void walk_tau32_tiled(const DepositArgs &a, const Tau
 // of the sightline from a shared counter (dynamic balance: pair costs differ by
 // orders of magnitude); each lane sets up one pair of the chunk into the warp's
 // staging area, then the warp walks the chunk's pairs one after another.
-template <bool COUNT>
+template <bool COUNT, bool REC>
 __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, long long e0,
                                                 long long e1, int S, unsigned long long *lo,
                                                 unsigned long long *hi, unsigned long long *tlo,
@@ -1500,20 +1607,52 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
         if (cb >= e1)
             break;
         const int n = (int)min((long long)chunk, e1 - cb);
-        if (lane < n) {
+        const PairRec *rec = REC ? reinterpret_cast<const PairRec *>(a.pl.rec) : nullptr;
+        if constexpr (REC) {
+            const int w = threadIdx.x >> 5;
+            unsigned long long *mbar = &s_stage_bar[w];
+            const unsigned mphase = s_stage_phase[w];
+            // the chunk's records land in the warp's staging area (n x 32 bytes:
+            // 16-byte aligned at both ends, within the chunk x 80-byte area)
+            PairRec *rb = reinterpret_cast<PairRec *>(sw);
+            fence_proxy_async_shared();   // earlier reads of the area come first
+            __syncwarp();
+            if (lane == 0)
+                bulk_copy_g2s(rb, rec + cb, (unsigned)n * (unsigned)sizeof(PairRec), mbar);
+            bool landed = mbar_wait(mbar, mphase, STAGE_WAIT_TRIES);
+            if (!landed) {
+                if (lane == 0)
+                    atomicOr(a.dev_err, (unsigned)DEVERR_STAGE_WAIT);
+                landed = mbar_wait(mbar, mphase, STAGE_WAIT_TRIES);
+            }
+            PairRec r{};
+            if (lane < n && landed)
+                r = rb[lane];
+            __syncwarp();
+            if (lane == 0)
+                s_stage_phase[w] = mphase ^ 1u;
+            if (lane < n) {
+                Stage32 st;
+                if (!landed || !stage32_setup(a.lp, rec_input(r), bintov_d, st, nullptr))
+                    st.flags = STAGE_SKIP;
+                sw[lane] = st;
+            }
+        } else if (lane < n) {
             const PairInput in = load_pair(a.p, a.pl, cb + lane, axis, true, a.dev_err);
             Stage32 st;
             if (!stage32_setup(a.lp, in, bintov_d, st, nullptr))
                 st.flags = STAGE_SKIP;
             sw[lane] = st;
         }
+        (void)rec;
         __syncwarp();
         for (int k = 0; k < n; k++) {
             const Stage32 st = sw[k];
             if (st.flags & STAGE_SKIP)
                 continue;
             if (st.flags & STAGE_CAREFUL) {
-                const PairInput in = load_pair(a.p, a.pl, cb + k, axis, true, a.dev_err);
+                const PairInput in = REC ? rec_input(rec[cb + k])
+                                         : load_pair(a.p, a.pl, cb + k, axis, true, a.dev_err);
                 walk_tau_careful<COUNT>(a, in, S, lo, hi, bad, lane, ct);
                 continue;
             }
@@ -1594,7 +1733,9 @@ __device__ __forceinline__ void deposit_pairs_col32(const DepositArgs &a, int ax
 // optical-depth deposit has 512-, 768- and 1024-thread builds (128, 80 and 64
 // registers per thread: 16, 24 or 32 warps per SM with the sightline's
 // accumulators on chip); the autotuner picks among them.
-template <bool TAU, int PREC, bool COUNT, int MAXT = (PREC == 0 ? 256 : 512)>
+// REC: the FP32 optical-depth deposit through pair records (PairRec; the
+// buffer is a.pl.rec) instead of gathering from the particle arrays.
+template <bool TAU, int PREC, bool COUNT, int MAXT = (PREC == 0 ? 256 : 512), bool REC = false>
 __global__ void __launch_bounds__(MAXT, 1)
     deposit_kernel(DepositArgs a)
 {
@@ -1605,6 +1746,16 @@ __global__ void __launch_bounds__(MAXT, 1)
     __shared__ unsigned s_ticket, s_chunk;
     const int nbins = a.lp.nbins;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    PairRec *rec = nullptr;
+    if constexpr (REC) {
+        static_assert(TAU && PREC == 1 && !COUNT, "records serve the FP32 optical depth");
+        rec = reinterpret_cast<PairRec *>(a.pl.rec);
+        if (lane == 0) {
+            mbar_init(&s_stage_bar[warp], 1);
+            s_stage_phase[warp] = 0u;
+        }
+        __syncthreads();
+    }
     const double boxtokpc = a.lp.vbox / nbins / a.lp.velfac;
     const double bintov_d = a.lp.vbox / nbins;
     Counters ct{};
@@ -1637,15 +1788,28 @@ __global__ void __launch_bounds__(MAXT, 1)
         const int axis = a.t.axis[line];
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
         // 1. fixed-point scale from an upper bound of the sightline total
-        const double B = order_free_bound(e0, e1, [&](long long e) {
+        const auto bf = [&](long long e) {
             const PairInput in = load_pair(a.p, a.pl, e, axis, TAU, a.dev_err);
-            if constexpr (TAU && PREC == 1)
+            if constexpr (REC) {
+                rec[e] = make_rec(in, a.pl.part[e]);   // for the second pass and the staging
+                return tau_pair_bound32(bk, in);
+            } else if constexpr (TAU && PREC == 1)
                 return tau_pair_bound32(bk, in);
             else if constexpr (!TAU && PREC == 1)
                 return colden_pair_bound32(a.lp, in, btk_abs, col_kfac);
             else
                 return TAU ? tau_pair_bound(a.lp, in) : colden_pair_bound(a.lp, in, boxtokpc);
-        }, &red);
+        };
+        double B;
+        if constexpr (REC) {
+            B = order_free_bound(e0, e1, bf, [&](long long e) {
+                return tau_pair_bound32(bk, rec_input(rec[e]));
+            }, &red);
+            // the records are read by bulk copies (async proxy) after the barrier below
+            fence_proxy_async_global();
+        } else {
+            B = order_free_bound(e0, e1, bf, bf, &red);
+        }
         if (threadIdx.x == 0)
             s_bad = !isfinite(B);
         unsigned long long *lo, *hi;
@@ -1672,7 +1836,7 @@ __global__ void __launch_bounds__(MAXT, 1)
         // 2. deposit: warp per pair
         if constexpr (TAU && PREC == 1) {
             if (!s_bad && B > 0.0)
-                deposit_pairs32<COUNT>(a, axis, e0, e1, S, lo, hi, tlo, thi, &s_bad,
+                deposit_pairs32<COUNT, REC>(a, axis, e0, e1, S, lo, hi, tlo, thi, &s_bad,
                                        stage + warp * a.chunk, &s_chunk, vtab, bintov_d, lane,
                                        ct);
         } else if constexpr (!TAU && PREC == 1) {
@@ -1883,11 +2047,12 @@ __global__ void __launch_bounds__(PREC == 0 ? 256 : 512) colden_channels_kernel(
         const long long e0 = a.pl.off[line], e1 = a.pl.off[line + 1];
         // 1. per-channel bounds, summed exactly as the single-channel deposit sums them
         for (int c = 0; c < nch; c++) {
-            const double B = order_free_bound(e0, e1, [&](long long e) {
+            const auto bf = [&](long long e) {
                 const PairInput in = load_pair_ch(a, e, axis, c);
                 return PREC == 1 ? colden_pair_bound32(a.lp, in, btk_abs, col_kfac)
                                  : colden_pair_bound(a.lp, in, btk);
-            }, &red);
+            };
+            const double B = order_free_bound(e0, e1, bf, bf, &red);
             if (threadIdx.x == 0) {
                 s_B[c] = B;
                 s_bad[c] = !isfinite(B);
@@ -2308,30 +2473,41 @@ int g_max_smem_optin = -1;
 
 // The kernel build for a block size: the FP32 tau form (not counting) has
 // 768- and 1024-thread builds beside the default.
+// The kernel build for a block size and input path: the FP32 optical-depth
+// deposit has 512-, 768- and 1024-thread builds, each gathering the particle
+// fields or reading pair records.
 template <bool TAU, int PREC, bool COUNT>
-decltype(&deposit_kernel<TAU, PREC, COUNT>) deposit_build(int threads)
+decltype(&deposit_kernel<TAU, PREC, COUNT>) deposit_build(int threads, bool rec)
 {
     if constexpr (TAU && PREC == 1 && !COUNT) {
+        if (rec) {
+            if (threads > 768)
+                return deposit_kernel<TAU, PREC, COUNT, 1024, true>;
+            if (threads > 512)
+                return deposit_kernel<TAU, PREC, COUNT, 768, true>;
+            return deposit_kernel<TAU, PREC, COUNT, 512, true>;
+        }
         if (threads > 768)
-            return deposit_kernel<TAU, PREC, COUNT, 1024>;
+            return deposit_kernel<TAU, PREC, COUNT, 1024, false>;
         if (threads > 512)
-            return deposit_kernel<TAU, PREC, COUNT, 768>;
+            return deposit_kernel<TAU, PREC, COUNT, 768, false>;
     }
+    (void)rec;
     return deposit_kernel<TAU, PREC, COUNT>;
 }
 
 template <bool TAU, int PREC, bool COUNT>
 void launch_one(const DepositArgs &a, int grid, int threads, size_t smem, cudaStream_t s)
 {
-    auto k = deposit_build<TAU, PREC, COUNT>(threads);
+    auto k = deposit_build<TAU, PREC, COUNT>(threads, a.pl.rec != nullptr);   // launcher: cfg.rec
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<grid, threads, smem, s>>>(a);
 }
 
 template <bool TAU, int PREC, bool COUNT>
-int resident_ctas(int threads, size_t smem)
+int resident_ctas(int threads, size_t smem, bool rec)
 {
-    auto k = deposit_build<TAU, PREC, COUNT>(threads);
+    auto k = deposit_build<TAU, PREC, COUNT>(threads, rec);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem);
@@ -2422,10 +2598,10 @@ int deposit_resident_ctas(const DepositLaunch &cfg, int compute_tau, int nbins)
     const size_t smem = deposit_smem_bytes(cfg, compute_tau, nbins);
     const int threads = cfg.threads;
     if (compute_tau)
-        return cfg.precision ? resident_ctas<true, 1, false>(threads, smem)
-                             : resident_ctas<true, 0, false>(threads, smem);
-    return cfg.precision ? resident_ctas<false, 1, false>(threads, smem)
-                         : resident_ctas<false, 0, false>(threads, smem);
+        return cfg.precision ? resident_ctas<true, 1, false>(threads, smem, cfg.rec != 0)
+                             : resident_ctas<true, 0, false>(threads, smem, false);
+    return cfg.precision ? resident_ctas<false, 1, false>(threads, smem, false)
+                         : resident_ctas<false, 0, false>(threads, smem, false);
 }
 
 int launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p,
@@ -2454,6 +2630,9 @@ int launch_deposit(const LineParams &lp, const LineTables &t, const Particles &p
     a.persistent = cfg.persistent;
     a.chunk = cfg.chunk;
     a.tiles = cfg.tiles;
+    // records only for the launch that asked for them (the buffer may be shared)
+    if (!(cfg.rec && cfg.precision == 1 && lp.compute_tau && counters == nullptr))
+        a.pl.rec = nullptr;
     const size_t smem = deposit_smem_bytes(cfg, lp.compute_tau, lp.nbins);
     int launched = 1;
     if (cfg.tiles && counters == nullptr) {

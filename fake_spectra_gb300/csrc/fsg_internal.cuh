@@ -43,6 +43,7 @@ enum DeviceError : unsigned {
     DEVERR_PAIR_COUNT = 8u,       // emit pass wrote fewer pairs of a sightline than counted
     DEVERR_PAIR_INDEX = 16u,      // a pair names a particle outside [0, n) (pair skipped)
     DEVERR_VORONOI_CELL = 32u,    // a Voronoi cell's points along a sightline are not contiguous
+    DEVERR_STAGE_WAIT = 64u,      // a staged copy of pair records did not complete in time
 };
 
 // Names of the set bits, for error messages ("fixed-point overflow, ...").
@@ -51,9 +52,10 @@ inline std::string deverr_text(unsigned bits)
     static const char *names[] = {"fixed-point overflow", "pair slot overflow",
                                   "window or sub-sample limit", "pair count mismatch",
                                   "pair particle index out of range",
-                                  "non-contiguous Voronoi cell along a sightline"};
+                                  "non-contiguous Voronoi cell along a sightline",
+                                  "staged pair-record copy timed out"};
     std::string r;
-    for (int b = 0; b < 6; b++)
+    for (int b = 0; b < 7; b++)
         if (bits & (1u << b))
             r += (r.empty() ? "" : ", ") + std::string(names[b]);
     return r.empty() ? "unknown" : r;
@@ -150,6 +152,9 @@ struct PairLists {
     const int *part;         // [P]
     const double *dr2;       // [P]
     const float2 *seg = nullptr;   // [P] Voronoi cell segments (kernel 2), else null
+    // [P] 32-byte pair records of the FP32 optical-depth deposit (written by
+    // its bound pass, read by the deposit), or null: gather from the particles
+    void *rec = nullptr;
 };
 
 // Host launchers (stream-ordered; no synchronisation inside).
@@ -245,6 +250,7 @@ struct DepositLaunch {
     int chunk;               // pairs staged per warp (FP32 form), else 0
     int tiles;               // in: allow far-field tiles (FP32 tau); out: planned
     int tiles_asked;         // what the caller allowed (tiles before planning)
+    int rec;                 // FP32 tau: through pair records (PairLists::rec must be set)
 };
 
 // Deposits all pairs of all sightlines into out[L*nbins] (pre-zeroed).  Lines

@@ -43,11 +43,12 @@ def _bind_stream(ctx):
 def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, atime, lam, gamma,
                                 fosc, amumass, tautail, pos, vel, dens, temp, h, axis, cofm,
                                 out=None, precision="fp64", threads=0, persistent=-1,
-                                count_work=False, far_tiles=True, chunk=0, tune=0):
+                                count_work=False, far_tiles=True, chunk=0, tune=0, records=-1):
     """`_Particle_Interpolate` on device tensors; returns `out` (nlos, nbins) float64 on device.
     far_tiles=False deposits the far damping wing of the FP32 form pixel by pixel.
-    threads/chunk/persistent left at 0/0/-1 take the autotuner's launch in the
-    FP32 form (tune: 0 cached, 1 time again, -1 library defaults)."""
+    threads/chunk/persistent/records left at 0/0/-1/-1 take the autotuner's
+    launch in the FP32 form (tune: 0 cached, 1 time again, -1 library defaults);
+    records=1 routes the FP32 optical depth through staged pair records."""
     import torch
     axis, cofm = _host_tables(axis, cofm)
     nlos = int(axis.shape[0])
@@ -60,7 +61,8 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
               _dptr(temp, "float32", "temp") if compute_tau else None,
               _dptr(h, "float32", "h")]
     _bind_stream(ctx)
-    opt = _lib.make_options(precision, threads, persistent, count_work, far_tiles, chunk, tune)
+    opt = _lib.make_options(precision, threads, persistent, count_work, far_tiles, chunk, tune,
+                            records)
     eb = _lib.errbuf()
     L = _lib.load()
     rc = L.fsg_particle_interpolate_device(
@@ -75,7 +77,7 @@ def particle_interpolate_device(ctx, compute_tau, nbins, kernel, box, velfac, at
 
 def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, vel, temp, h,
                          axis, cofm, lines, precision="fp32", threads=0, persistent=-1, chunk=0,
-                         tune=0):
+                         tune=0, records=-1):
     """Several absorption lines in one call (one sightline search, one CUDA graph).
 
     lines: sequence of (transition, dens, want_tau, want_colden) with
@@ -101,7 +103,8 @@ def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, v
         arr[k].colden = _dptr(col, "float64", "colden") if col is not None else None
         outs.append((tau, col))
     _bind_stream(ctx)
-    opt = _lib.make_options(precision, threads, persistent, chunk=chunk, tune=tune)
+    opt = _lib.make_options(precision, threads, persistent, chunk=chunk, tune=tune,
+                            records=records)
     eb = _lib.errbuf()
     L = _lib.load()
     rc = L.fsg_spectra_batch_device(

@@ -57,7 +57,10 @@ typedef struct {
                        timed on a sample of the call's sightlines the first
                        time the class is met, then cached; 1 = time again now;
                        -1 = library defaults, no tuning                       */
-    int reserved;
+    int records;    /* FP32 optical depths: 1 = through 32-byte pair records
+                       written by the deposit's bound pass and staged per warp
+                       with bulk asynchronous copies; 0 = gather the particle
+                       fields; -1 = tuned (FP32 form) or 0                    */
 } fsg_options;
 
 typedef struct {
@@ -87,7 +90,7 @@ typedef struct {
     int32_t tune_ran;            /* 1: the autotuner timed candidates in this call */
     int32_t tune_candidates;     /* candidates timed by that run */
     int32_t tune_sample_lines;   /* sightlines of its timing sample */
-    int32_t reserved2;
+    int32_t launch_records;      /* 1: the deposit went through pair records */
     double tune_ms_default;      /* deposit of the sample with the library defaults */
     double tune_ms_best;         /* ... with the chosen launch */
     /* host-pointer entry points: the host->device copies of the inputs and the
@@ -301,7 +304,7 @@ typedef struct {
 } fsg_tune_key;
 
 typedef struct {
-    int32_t threads, chunk, persistent;
+    int32_t threads, chunk, persistent, records;   /* the chosen launch (fsg_options) */
     int32_t candidates, sample_lines;
     double ms_default, ms_best;
 } fsg_tune_entry;

@@ -32,12 +32,14 @@ def test_every_launch_gives_the_same_bits(ctx, compute_tau, nbins):
     want = I.particle_interpolate_device(ctx, *a, precision="fp32", tune=-1)
     launches = [(512, 4, 1), (512, 16, 1), (512, 8, 0), (384, 8, 1), (256, 8, 1), (256, 4, 1),
                 (128, 1, 1), (512, 32, 1)]
-    if compute_tau:   # the 768- and 1024-thread builds of the optical-depth kernel
-        launches += [(768, 8, 1), (768, 4, 1), (1024, 4, 1), (1024, 8, 0)]
-    for threads, chunk, persistent in launches:
+    launches = [l + (0,) for l in launches]
+    if compute_tau:   # the 768- and 1024-thread builds, gathering or through pair records
+        launches += [(768, 8, 1, 0), (768, 4, 1, 0), (1024, 4, 1, 0), (1024, 8, 0, 0),
+                     (512, 8, 1, 1), (768, 8, 1, 1), (1024, 8, 1, 1), (1024, 4, 0, 1)]
+    for threads, chunk, persistent, records in launches:
         got = I.particle_interpolate_device(ctx, *a, precision="fp32", threads=threads,
-                                            chunk=chunk, persistent=persistent)
-        assert torch.equal(got, want), (threads, chunk, persistent)
+                                            chunk=chunk, persistent=persistent, records=records)
+        assert torch.equal(got, want), (threads, chunk, persistent, records)
     w64 = I.particle_interpolate_device(ctx, *a, precision="fp64")
     for threads, persistent in [(128, 0), (256, 1), (64, 1)]:
         got = I.particle_interpolate_device(ctx, *a, precision="fp64", threads=threads,

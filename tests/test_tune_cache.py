@@ -27,9 +27,9 @@ def fresh(tmp_path):
 def test_store_and_lookup_by_class(fresh):
     assert _lib.tune_cache_lookup(_key()) is None
     _lib.tune_cache_store(_key(), 384, 4, 1, ms_default=10.0, ms_best=9.0, candidates=7,
-                          sample_lines=608)
+                          sample_lines=608, records=1)
     e = _lib.tune_cache_lookup(_key())
-    assert (e["threads"], e["chunk"], e["persistent"]) == (384, 4, 1)
+    assert (e["threads"], e["chunk"], e["persistent"], e["records"]) == (384, 4, 1, 1)
     assert e["ms_default"] == 10.0 and e["ms_best"] == 9.0 and e["candidates"] == 7
     # another class (other nbins bucket, other line) is a miss
     assert _lib.tune_cache_lookup(_key(nbins_b=20)) is None
@@ -44,7 +44,8 @@ def test_file_round_trip(fresh):
     # a line that does not parse, and one with an invalid launch, are skipped on load
     with open(path, "a") as f:
         f.write("garbage line\n")
-        f.write("fsg-tune-v1 152 1 1 1 26 18 26 15 -9 100 4 1 7 608 1.0 1.0\n")
+        f.write("fsg-tune-v2 152 1 1 1 26 18 26 15 -9 100 4 1 0 7 608 1.0 1.0\n")
+        f.write("fsg-tune-v2 152 1 1 1 26 18 26 15 -9 512 4 1 2 7 608 1.0 1.0\n")
     _lib.tune_cache_file(None)
     _lib.tune_cache_clear()
     assert _lib.tune_cache_lookup(_key()) is None
@@ -56,9 +57,10 @@ def test_file_round_trip(fresh):
     assert _lib.tune_cache_lookup(_key(damp_b=-9)) is None
 
 
-@pytest.mark.parametrize("threads,chunk,persistent", [(100, 8, 1), (512, 0, 1), (512, 33, 1),
-                                                       (2048, 8, 1), (512, 8, 2)])
-def test_invalid_launch_refused(fresh, threads, chunk, persistent):
+@pytest.mark.parametrize("threads,chunk,persistent,records", [
+    (100, 8, 1, 0), (512, 0, 1, 0), (512, 33, 1, 0), (2048, 8, 1, 0), (512, 8, 2, 0),
+    (512, 8, 1, 2)])
+def test_invalid_launch_refused(fresh, threads, chunk, persistent, records):
     with pytest.raises(ValueError):
-        _lib.tune_cache_store(_key(), threads, chunk, persistent)
+        _lib.tune_cache_store(_key(), threads, chunk, persistent, records=records)
     assert _lib.tune_cache_lookup(_key()) is None
