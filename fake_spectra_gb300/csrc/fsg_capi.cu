@@ -14,11 +14,13 @@
 #include "fsg_internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -32,6 +34,12 @@ using namespace fsg;
 namespace {
 
 struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+// Pinned host memory owned by a context (grow-only).
+struct HostBuf {
     void *p = nullptr;
     size_t cap = 0;
 };
@@ -87,6 +95,7 @@ struct fsg_context {
     DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
     DevBuf tune_order;                                       // autotuner sample
     DevBuf prec;                                             // pair records (FP32 tau)
+    HostBuf hstage;   // host-pointer entries: pinned staging of inputs and output
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t cp[2] = {nullptr, nullptr};   // copy timing of the host-pointer entries
     // host-pointer entries: the inputs the search does not read are uploaded on
@@ -121,8 +130,28 @@ struct fsg_context {
         return b.p;
     }
 
+    void *ensure_host(HostBuf &b, size_t bytes)
+    {
+        if (bytes == 0)
+            bytes = 16;
+        if (b.cap < bytes) {
+            if (b.p)
+                cuda_check(cudaFreeHost(b.p), "cudaFreeHost");
+            b.p = nullptr;
+            b.cap = 0;
+            const size_t want = bytes + bytes / 8;
+            cuda_check(cudaHostAlloc(&b.p, want, cudaHostAllocDefault), "cudaHostAlloc");
+            b.cap = want;
+        }
+        return b.p;
+    }
+
     void release_all()
     {
+        if (hstage.p)
+            cudaFreeHost(hstage.p);
+        hstage.p = nullptr;
+        hstage.cap = 0;
         DevBuf *bufs[] = {&pos, &vel, &dens, &temp, &hh, &out, &key, &second, &axis, &pack,
                           &cell_start[0], &cell_start[1], &cell_start[2], &cell_line[0],
                           &cell_line[1], &cell_line[2], &line_count, &cursor, &off, &part, &dr2,
@@ -925,38 +954,44 @@ void ctx_init(fsg_context *c, int device)
         cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 }
 
-// Writes zeros over a caller's host output from a few threads while the GPU
-// works.  A fresh allocation (NumPy's zeros, calloc) has no pages yet; without
-// this the device-to-host copy at the end of the call faults them in one by
-// one, which on this machine costs more than the copy itself.
-class PreTouch {
-  public:
-    PreTouch(void *p, size_t bytes)
-    {
-        if (!p || bytes < (64u << 20))
-            return;
-        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        const size_t n = std::min<size_t>(8, std::max<size_t>(1, hw / 2));
-        const size_t chunk = (bytes / n + 4095) & ~(size_t)4095;
-        for (size_t i = 0; i < n; i++) {
-            const size_t off = i * chunk;
-            if (off >= bytes)
-                break;
-            const size_t len = std::min(chunk, bytes - off);
-            threads_.emplace_back([p, off, len] { memset((char *)p + off, 0, len); });
-        }
+// Copies n bytes between host buffers with up to `threads` threads (pieces
+// of at least 8 MiB).  The host-pointer entry points move the caller's arrays
+// through the context's pinned staging memory: the GPU's copy engines read
+// and write only that warm, pinned memory, whose transfer rate does not
+// depend on how the caller allocated its arrays (on the GPU machine, copies
+// straight from or to callers' buffers ran at 11-60 GB/s instead of about
+// 200 GB/s, and slowed down from call to call), and the caller's pages are
+// only ever touched by these CPU threads.
+void parallel_copy(void *dst, const void *src, size_t n, unsigned threads)
+{
+    if (n == 0)
+        return;
+    const size_t min_piece = 8u << 20;
+    size_t k = std::max<size_t>(1, std::min<size_t>(threads, (n + min_piece - 1) / min_piece));
+    if (k == 1) {
+        memcpy(dst, src, n);
+        return;
     }
-    void wait()
-    {
-        for (auto &t : threads_)
-            t.join();
-        threads_.clear();
+    const size_t piece = ((n + k - 1) / k + 63) & ~(size_t)63;
+    std::vector<std::thread> pool;
+    for (size_t i = 1; i < k; i++) {
+        const size_t off = i * piece;
+        if (off >= n)
+            break;
+        const size_t len = std::min(piece, n - off);
+        pool.emplace_back([dst, src, off, len] {
+            memcpy((char *)dst + off, (const char *)src + off, len);
+        });
     }
-    ~PreTouch() { wait(); }
+    memcpy(dst, src, std::min(piece, n));
+    for (auto &t : pool)
+        t.join();
+}
 
-  private:
-    std::vector<std::thread> threads_;
-};
+unsigned copy_threads()
+{
+    return std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+}
 
 // The per-device context of the host-pointer entry points (created on first
 // use; the caller holds g_default_mu).
@@ -1056,14 +1091,14 @@ void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, dou
                      double velfac, double lambda, double gamma, double fosc, double amumass,
                      double tautail, const Particles &p, const int32_t *axis, const double *cofm,
                      int32_t nlos, double *out, const fsg_options *opt,
-                     cudaEvent_t inputs_ready = nullptr)
+                     const std::function<void()> &before_deposit = nullptr)
 {
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
     build_tables(c, axis, cofm, nlos, box);
     search_pairs(c, p, nlos);
     // the inputs only the deposit reads may still be on their way (host-pointer entry)
-    if (inputs_ready)
-        cuda_check(cudaStreamWaitEvent(c->stream, inputs_ready, 0), "wait for uploads");
+    if (before_deposit)
+        before_deposit();
     LineParams lp = make_line_params(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
                                      amumass, tautail);
     const float2 *seg = kernel == VORONOI ? voronoi_cells(c, p, cofm, box) : nullptr;
@@ -1211,58 +1246,97 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         fsg_context *c = default_context();
         cudaStream_t s = c->stream;
         const size_t n3 = sizeof(float) * 3 * (size_t)npart, n1 = sizeof(float) * (size_t)npart;
-        auto up = [&](DevBuf &b, const void *src, size_t bytes) -> const float * {
-            void *d = c->ensure(b, bytes);
-            if (bytes)
-                cuda_check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s), "H2D");
-            return (const float *)d;
-        };
-        // no copy of the caller's arrays may outlive the call, error returns included
-        struct SideSync {
+        const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
+        // pinned staging: pos | h | dens | vel | temp | out (256-byte aligned parts)
+        const auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t o_h = al(n3), o_dens = o_h + al(n1), o_vel = o_dens + al(n1);
+        const size_t o_temp = o_vel + (compute_tau ? al(n3) : 0);
+        const size_t o_out = o_temp + (compute_tau ? al(n1) : 0);
+        char *hs = (char *)c->ensure_host(c->hstage, o_out + al(nout));
+        const unsigned nthr = copy_threads();
+        // the helper thread stages what only the deposit reads while the search runs;
+        // it is joined on every path, and no copy of the caller's arrays outlives
+        // the call (error returns included)
+        std::thread helper;
+        std::string helper_err;
+        struct Guard {
             fsg_context *c;
-            ~SideSync()
+            std::thread &t;
+            ~Guard()
             {
+                if (t.joinable())
+                    t.join();
                 cudaStreamSynchronize(c->side);
                 cudaStreamSynchronize(c->stream);
             }
-        } side_sync{c};
+        } guard{c, helper};
         Particles p;
         p.n = npart;
-        // the search reads pos and h: they go first; vel, dens and temp follow on
-        // the side stream while the search runs (the deposit waits for them)
+        auto *dpos = (float *)c->ensure(c->pos, n3);
+        auto *dh = (float *)c->ensure(c->hh, n1);
+        auto *ddens = (float *)c->ensure(c->dens, n1);
+        auto *dvel = compute_tau ? (float *)c->ensure(c->vel, n3) : nullptr;
+        auto *dtemp = compute_tau ? (float *)c->ensure(c->temp, n1) : nullptr;
+        p.pos = dpos;
+        p.hh = dh;
+        p.dens = ddens;
+        p.vel = dvel;
+        p.temp = dtemp;
+        // the search reads pos and h: staged and sent first
         cuda_check(cudaEventRecord(c->cp[0], s), "event");
-        p.pos = up(c->pos, pos, n3);
-        p.hh = up(c->hh, h, n1);
-        cuda_check(cudaEventRecord(c->up[0], s), "event");
-        cuda_check(cudaStreamWaitEvent(c->side, c->up[0], 0), "order uploads");
-        const auto up_side = [&](DevBuf &b, const void *src, size_t bytes) -> const float * {
-            void *d = c->ensure(b, bytes);
-            if (bytes)
-                cuda_check(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, c->side),
-                           "H2D");
-            return (const float *)d;
+        parallel_copy(hs, pos, n3, nthr);
+        parallel_copy(hs + o_h, h, n1, nthr);
+        if (npart > 0) {
+            cuda_check(cudaMemcpyAsync(dpos, hs, n3, cudaMemcpyHostToDevice, s), "H2D");
+            cuda_check(cudaMemcpyAsync(dh, hs + o_h, n1, cudaMemcpyHostToDevice, s), "H2D");
+        }
+        helper = std::thread([&] {
+            const cudaError_t e0 = cudaSetDevice(c->device);
+            if (e0 != cudaSuccess) {
+                helper_err = cudaGetErrorString(e0);
+                return;
+            }
+            parallel_copy(hs + o_dens, dens, n1, nthr);
+            if (compute_tau) {
+                parallel_copy(hs + o_vel, vel, n3, nthr);
+                parallel_copy(hs + o_temp, temp, n1, nthr);
+            }
+            cudaError_t e = cudaSuccess;
+            if (npart > 0) {
+                e = cudaMemcpyAsync(ddens, hs + o_dens, n1, cudaMemcpyHostToDevice, c->side);
+                if (e == cudaSuccess && compute_tau)
+                    e = cudaMemcpyAsync(dvel, hs + o_vel, n3, cudaMemcpyHostToDevice, c->side);
+                if (e == cudaSuccess && compute_tau)
+                    e = cudaMemcpyAsync(dtemp, hs + o_temp, n1, cudaMemcpyHostToDevice,
+                                        c->side);
+            }
+            if (e == cudaSuccess)
+                e = cudaEventRecord(c->up[1], c->side);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(c->cp[1], c->side);
+            if (e != cudaSuccess)
+                helper_err = cudaGetErrorString(e);
+        });
+        const auto inputs_ready = [&] {
+            helper.join();
+            if (!helper_err.empty())
+                fail(FSG_ERR_CUDA, "staging the inputs: %s", helper_err.c_str());
+            cuda_check(cudaStreamWaitEvent(s, c->up[1], 0), "wait for uploads");
         };
-        p.dens = up_side(c->dens, dens, n1);
-        p.vel = compute_tau ? up_side(c->vel, vel, n3) : nullptr;
-        p.temp = compute_tau ? up_side(c->temp, temp, n1) : nullptr;
-        cuda_check(cudaEventRecord(c->up[1], c->side), "event");
-        cuda_check(cudaEventRecord(c->cp[1], c->side), "event");
-        const size_t nout = sizeof(double) * (size_t)nlos * (size_t)(nbins > 0 ? nbins : 0);
         double *dout = (double *)c->ensure(c->out, nout);
-        PreTouch touch(out, nout);
         run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
-                        tautail, p, axis, cofm, nlos, dout, opt, c->up[1]);
+                        tautail, p, axis, cofm, nlos, dout, opt, inputs_ready);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
-        c->stats.ms_h2d = ms;   // from the first upload to the last (search overlapped)
-        touch.wait();
-        cuda_check(cudaEventRecord(c->cp[0], s), "event");
+        c->stats.ms_h2d = ms;   // first staging copy to the last upload (search overlapped)
+        const auto t0 = std::chrono::steady_clock::now();
         if (nout)
-            cuda_check(cudaMemcpyAsync(out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaEventRecord(c->cp[1], s), "event");
+            cuda_check(cudaMemcpyAsync(hs + o_out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
         cuda_check(cudaStreamSynchronize(s), "D2H");
-        cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
-        c->stats.ms_d2h = ms;
+        parallel_copy(out, hs + o_out, nout, nthr);
+        c->stats.ms_d2h =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                .count();   // device-to-staging copy and the copy into the caller's array
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);
