@@ -25,6 +25,7 @@ Multi-GPU: independent replicas (the path is not sharded), weak scaling.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -61,12 +62,17 @@ TRAFFIC_WRITE_PER_PIXEL = 0.174416896e9 / (2048 * 11152)
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
+FALLBACK_HBM_GBS = 6800.0   # one earlier STREAM-style copy measurement on a GB300
+
+
 def measured_hbm_gbs():
+    """(GB/s, source): the measured copy bandwidth of MEASURED_PEAKS.json, else
+    the fallback figure."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f).get("hbm_gbs"))
+            return float(json.load(f).get("hbm_gbs")), "measured (MEASURED_PEAKS.json)"
     except Exception:
-        return None
+        return FALLBACK_HBM_GBS, "fallback (no MEASURED_PEAKS.json)"
 
 
 def search_roofline(npart, npairs, nlos, ms):
@@ -76,10 +82,10 @@ def search_roofline(npart, npairs, nlos, ms):
     (8 B); count and emit: read the order (4 B), pos (12 B) and h (4 B) each;
     emit: write 12 B per pair; offsets 8 B per sightline."""
     algo = npart * (12 + 4 + 8 + 2 * (4 + 12 + 4)) + npairs * 12 + nlos * 8
-    hbm = measured_hbm_gbs()
+    hbm, src = measured_hbm_gbs()
     achieved = algo / (ms * 1e-3) / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm if hbm else None, "bytes": algo,
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "peak_source": src,
+            "unit": "GB/s", "frac": achieved / hbm, "bytes": algo,
             "note": "the search is limited by the cell walk (latency of the dependent cell "
                     "and sightline loads), not by HBM (16 B of particle data per particle "
                     "per pass); the FP64 predicate runs only on the thin shell the float "
@@ -804,7 +810,7 @@ def main():
 
         # ---- flux statistics of the FP32 tau still in HBM (HBM-bound reductions)
         from fake_spectra_gb300 import fluxstatistics as fstat
-        hbm = measured_hbm_gbs()
+        hbm, hbm_src = measured_hbm_gbs()
         ntau = tau32.numel()
 
         def timed(fn):
@@ -817,13 +823,27 @@ def main():
         fstat._context()
         scale, ms_mf = timed(lambda: fstat.mean_flux(tau32, 0.7))
         _, ms_pdf = timed(lambda: fstat.flux_pdf(tau32, 20, None))
+        pdf_kernel_ms = fstat._context().stats()["ms_flux"]
         _, ms_pow = timed(lambda: fstat.flux_power(tau32, w.nbins * 1.0, 8, None, False))
+        power_kernels_ms = fstat._context().stats()["ms_flux"]
+        nspec, npix = tau32.shape
+        # the usual flop count of a complex transform of length n, 5 n log2 n,
+        # per pair of sightlines
+        fft_flops = 5.0 * npix * math.log2(npix) * ((nspec + 1) // 2)
         res["flux_statistics"] = {
             "tau_pixels": ntau, "mean_flux_ms": ms_mf, "scale": scale,
             "flux_pdf_ms": ms_pdf, "flux_power_ms": ms_pow,
-            "pdf_hbm_frac": (ntau * 8 / (ms_pdf * 1e-3) / 1e9) / hbm if hbm else None,
-            "note": "wall time of each call (host API, tau resident in HBM); the PDF pass reads "
-                    "8 B per pixel once, against the measured HBM copy bandwidth"}
+            "pdf_kernel_ms": pdf_kernel_ms,
+            "pdf_kernel_hbm_frac": (ntau * 8 / (pdf_kernel_ms * 1e-3) / 1e9) / hbm,
+            "power_kernels_ms": power_kernels_ms,
+            "power_fft_gflops": fft_flops / (power_kernels_ms * 1e-3) / 1e9,
+            "hbm_peak_gbs": hbm, "hbm_peak_source": hbm_src,
+            "note": "wall time of each call (host API, tau resident in HBM); pdf_kernel_ms is "
+                    "the histogram kernel's device time (8 B of tau per pixel, read once); "
+                    "power_kernels_ms the device time of the power's own kernels (pack with "
+                    "the FP64 exponentials, transform passes, ordered power sums), without "
+                    "the mean-flux pass that flux_power_ms includes; power_fft_gflops counts "
+                    "5 n log2 n flops per complex transform of a sightline pair"}
 
     # ---- differentiation form: forward and forward+backward on the 128^3 workload
     if not args.no_bwd:

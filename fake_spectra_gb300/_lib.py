@@ -76,7 +76,7 @@ class Stats(ctypes.Structure):
                 ("launch_tuned", _c_i32), ("tune_ran", _c_i32), ("tune_candidates", _c_i32),
                 ("tune_sample_lines", _c_i32), ("launch_records", _c_i32),
                 ("tune_ms_default", _c_d), ("tune_ms_best", _c_d), ("ms_h2d", _c_d),
-                ("ms_d2h", _c_d)]
+                ("ms_d2h", _c_d), ("ms_flux", _c_d)]
 
 
 class TuneKey(ctypes.Structure):
@@ -277,7 +277,7 @@ def _stats_dict(s):
                      "sample_lines": int(s.tune_sample_lines),
                      "ms_default": float(s.tune_ms_default),
                      "ms_best": float(s.tune_ms_best)},
-            "ms_h2d": float(s.ms_h2d), "ms_d2h": float(s.ms_d2h)}
+            "ms_h2d": float(s.ms_h2d), "ms_d2h": float(s.ms_d2h), "ms_flux": float(s.ms_flux)}
 
 
 def fma_peak_tflops(precision="fp32"):

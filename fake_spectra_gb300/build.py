@@ -19,7 +19,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libfsg.so")
 
 SOURCES = ["fsg_capi.cu", "fsg_index.cu", "fsg_deposit.cu", "fsg_peak.cu", "fsg_noalloc.cu",
-           "fsg_flux.cu", "fsg_voronoi.cu"]
+           "fsg_flux.cu", "fsg_power.cu", "fsg_voronoi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -72,7 +72,7 @@ def build(force=False, verbose=False, ptxas_verbose=False):
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lcufft", "-lpthread"]
+        cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -9,7 +9,6 @@
 //   3. deposit: sightlines ordered by descending pair count; one kernel;
 //      sightlines with non-finite contributions re-run by the fallback kernel.
 #include "fsg.h"
-#include <cufft.h>
 
 #include "fsg_internal.cuh"
 
@@ -92,6 +91,8 @@ struct fsg_context {
     DevBuf skey, sperm, shist, sstart, ssums;                // particle ordering
     DevBuf flag, tcount, tstart, tsums, idx;                 // _near_lines
     DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
+    DevBuf ptables, pchirp, pbhat, ppart;                    // flux power plan and partials
+    PowerPlan pplan;                                         // plan of the last flux power call
     DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
     DevBuf tune_order;                                       // autotuner sample
     DevBuf prec;                                             // pair records (FP32 tau)
@@ -158,7 +159,9 @@ struct fsg_context {
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
-                          &ffft, &fpower, &vseg, &vscratch, &vcofm, &tune_order, &prec};
+                          &ffft, &fpower, &ptables, &pchirp, &pbhat, &ppart, &vseg, &vscratch,
+                          &vcofm, &tune_order, &prec};
+        pplan = PowerPlan{};
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -1667,8 +1670,9 @@ int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, do
     try {
         if (!ctx || !edges || !counts)
             fail(FSG_ERR_VALUE, "ctx, edges and counts must not be NULL");
-        if (n < 0 || nb < 1 || nb > 16384)
-            fail(FSG_ERR_VALUE, "need n >= 0 and 1 <= nbins <= 16384 (got %lld, %d)",
+        // the block histogram keeps 16 bytes of shared memory per bin
+        if (n < 0 || nb < 1 || nb > 8192)
+            fail(FSG_ERR_VALUE, "need n >= 0 and 1 <= nbins <= 8192 (got %lld, %d)",
                  (long long)n, nb);
         for (int j = 0; j < nb; j++)
             if (!(edges[j] < edges[j + 1]))
@@ -1680,14 +1684,19 @@ int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, do
         cuda_check(cudaMemcpyAsync(de, edges, sizeof(double) * (nb + 1), cudaMemcpyHostToDevice,
                                    s), "H2D");
         cuda_check(cudaMemsetAsync(dc, 0, sizeof(long long) * nb, s), "memset");
+        cuda_check(cudaEventRecord(ctx->ev[2], s), "event");
         if (n > 0) {
             launch_flux_hist(tau, n, scale, de, nb, dc, s);
             ctx->stats.gpu_launches++;
             cuda_check(cudaGetLastError(), "flux histogram launch");
         }
+        cuda_check(cudaEventRecord(ctx->ev[3], s), "event");
         cuda_check(cudaMemcpyAsync(counts, dc, sizeof(long long) * nb, cudaMemcpyDeviceToHost, s),
                    "D2H");
         cuda_check(cudaStreamSynchronize(s), "flux histogram");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+        ctx->stats.ms_flux = ms;
         return FSG_OK;
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);
@@ -1706,51 +1715,48 @@ int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, in
                  (long long)nspec, (long long)npix);
         cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
         cudaStream_t s = ctx->stream;
-        const int nk = (int)(npix / 2 + 1);
-        // rows per batched transform: about 256 MB of real input at a time
-        long long rows = (256ll << 20) / (8 * npix);
-        rows = rows < 1 ? 1 : (rows > nspec ? nspec : rows);
-        auto *dflux = (double *)ctx->ensure(ctx->fdflux, sizeof(double) * rows * npix);
-        auto *F = ctx->ensure(ctx->ffft, sizeof(cufftDoubleComplex) * rows * nk);
+        const long long nk = npix / 2 + 1;
+        PowerPlan &pl = ctx->pplan;
+        if (pl.npix != npix) {
+            pl = PowerPlan{};
+            PowerPlan fresh = power_plan(npix);
+            auto *tables = (double2 *)ctx->ensure(ctx->ptables,
+                                                  sizeof(double2) * (size_t)fresh.table_len);
+            double2 *chirp = nullptr, *bhat = nullptr, *scratch = nullptr;
+            if (fresh.bluestein) {
+                chirp = (double2 *)ctx->ensure(ctx->pchirp, sizeof(double2) * (size_t)npix);
+                bhat = (double2 *)ctx->ensure(ctx->pbhat, sizeof(double2) * (size_t)fresh.len);
+                scratch = (double2 *)ctx->ensure(ctx->ffft, sizeof(double2) * (size_t)fresh.len);
+            }
+            ctx->stats.gpu_launches += power_plan_tables(fresh, tables, chirp, bhat, scratch, s);
+            cuda_check(cudaGetLastError(), "flux power tables");
+            // the scratch buffer is regrown below
+            cuda_check(cudaStreamSynchronize(s), "flux power tables");
+            pl = fresh;
+        }
+        const long long chunk = power_pairs_per_chunk(pl, nspec);
+        const size_t words = sizeof(double2) * (size_t)chunk * (size_t)pl.len;
+        auto *a = (double2 *)ctx->ensure(ctx->fdflux, words);
+        auto *b = (double2 *)ctx->ensure(ctx->ffft, words);
+        auto *part = (double *)ctx->ensure(ctx->ppart, sizeof(double) * power_partials(npix));
         auto *dp = (double *)ctx->ensure(ctx->fpower, sizeof(double) * nk);
         cuda_check(cudaMemsetAsync(dp, 0, sizeof(double) * nk, s), "memset");
-        auto plan_for = [&](int batch) {
-            cufftHandle plan;
-            int n1 = (int)npix;
-            if (cufftPlanMany(&plan, 1, &n1, nullptr, 1, (int)npix, nullptr, 1, nk, CUFFT_D2Z,
-                              batch) != CUFFT_SUCCESS)
-                fail(FSG_ERR_CUDA, "cufftPlanMany failed");
-            if (cufftSetStream(plan, s) != CUFFT_SUCCESS) {
-                cufftDestroy(plan);
-                fail(FSG_ERR_CUDA, "cufftSetStream failed");
-            }
-            return plan;
-        };
-        cufftHandle plan = plan_for((int)rows);
-        long long plan_rows = rows;
-        try {
-            for (long long r0 = 0; r0 < nspec; r0 += rows) {
-                const long long r = (r0 + rows <= nspec) ? rows : nspec - r0;
-                if (r != plan_rows) {
-                    cufftDestroy(plan);
-                    plan = plan_for((int)r);
-                    plan_rows = r;
-                }
-                launch_dflux(tau + r0 * npix, r * npix, scale, 1.0 / mean_flux, dflux, s);
-                if (cufftExecD2Z(plan, dflux, (cufftDoubleComplex *)F) != CUFFT_SUCCESS)
-                    fail(FSG_ERR_CUDA, "cufftExecD2Z failed");
-                launch_power_accumulate(F, (int)r, nk, (int)npix, vmax, dp, s);
-                ctx->stats.gpu_launches += 2;
-                cuda_check(cudaGetLastError(), "flux power launch");
-            }
-        } catch (...) {
-            cufftDestroy(plan);
-            throw;
+        cuda_check(cudaEventRecord(ctx->ev[2], s), "event");
+        for (long long r0 = 0; r0 < nspec; r0 += 2 * chunk) {
+            const long long r = (r0 + 2 * chunk <= nspec) ? 2 * chunk : nspec - r0;
+            ctx->stats.gpu_launches += power_chunk(
+                pl, (const double2 *)ctx->ptables.p, (const double2 *)ctx->pchirp.p,
+                (const double2 *)ctx->pbhat.p, tau + r0 * npix, r, scale, 1.0 / mean_flux, vmax,
+                a, b, part, dp, s);
+            cuda_check(cudaGetLastError(), "flux power launch");
         }
-        cufftDestroy(plan);
+        cuda_check(cudaEventRecord(ctx->ev[3], s), "event");
         cuda_check(cudaMemcpyAsync(power, dp, sizeof(double) * nk, cudaMemcpyDeviceToHost, s),
                    "D2H");
         cuda_check(cudaStreamSynchronize(s), "flux power");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+        ctx->stats.ms_flux = ms;
         for (int k = 0; k < nk; k++)
             power[k] /= (double)nspec;
         return FSG_OK;

@@ -2324,7 +2324,9 @@ struct __align__(16) StageGrad {
     float scale_nod, temp;
     int ip, pad;
 };
-constexpr int GRAD_THREADS = 512, GRAD_CHUNK = 32;
+// 1024 threads at 64 registers (32 warps per SM; the kernel spills the same
+// ~250 bytes at 128 registers), 16 staged pairs per warp.
+constexpr int GRAD_THREADS = 1024, GRAD_CHUNK = 16;
 constexpr size_t GRAD_SMEM = (size_t)(GRAD_THREADS / 32) * GRAD_CHUNK * sizeof(StageGrad);
 
 // One warp, one FP32-walk pair: dL/d(dens), dL/d(v_los), dL/dT summed over the
@@ -2382,7 +2384,7 @@ __device__ __forceinline__ void grad_pair32(const Tau32 &s, const double *gt, in
 // Sightlines from a ticket queue; within a sightline the warps take chunks of
 // pairs from a shared counter, each lane sets up one pair of the chunk (the
 // forward's lane-parallel setup) and the warp walks them one after another.
-__global__ void __launch_bounds__(GRAD_THREADS) grad_kernel(GradArgs a)
+__global__ void __launch_bounds__(GRAD_THREADS, 1) grad_kernel(GradArgs a)
 {
     extern __shared__ __align__(16) unsigned char gsmem[];
     __shared__ float2 vtab[FSG_V32_N];

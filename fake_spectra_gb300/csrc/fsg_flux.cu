@@ -1,14 +1,11 @@
 // Flux statistics of optical depths still resident in HBM: the mean-flux
 // rescaling (fake_spectra/py_module.cpp:235-282, get_mean_flux_scale /
-// Py_mean_flux), the flux PDF (fake_spectra/fluxstatistics.py:42-51) and the
-// 1-D flux power spectrum (fluxstatistics.py:53-110).
+// Py_mean_flux) and the flux PDF (fake_spectra/fluxstatistics.py:42-51); the
+// 1-D flux power spectrum is in fsg_power.cu.
 //
-// All three read tau once per pass and are HBM-bound reductions.  Sums are
-// deterministic: every block reduces a fixed contiguous range in a fixed
-// order and a second pass adds the block partials in order, so a result does
-// not depend on scheduling.
-#include <cufft.h>
-
+// Each pass reads tau once.  Sums are deterministic: every block reduces a
+// fixed contiguous range in a fixed order and a second pass adds the block
+// partials in order, so a result does not depend on scheduling.
 #include "fsg_internal.cuh"
 
 namespace fsg {
@@ -213,28 +210,49 @@ __device__ __forceinline__ int hist_bin64(double x, const double *edges, int nb,
     return j;
 }
 
+// Adds one count to bin j (j < 0: none) of the warp's or the block's histogram;
+// lanes of the warp that hit the same bin add together (saturated spectra put
+// most pixels of a warp in the same bin).
+template <bool WARP_PRIVATE>
+__device__ __forceinline__ void hist_add(int j, unsigned *wh, unsigned long long *bh)
+{
+    const unsigned peers = __match_any_sync(0xffffffffu, j);
+    const int lane = threadIdx.x & 31;
+    if (j >= 0 && lane == __ffs(peers) - 1) {
+        if (WARP_PRIVATE)
+            atomicAdd(&wh[j], (unsigned)__popc(peers));
+        else
+            atomicAdd(&bh[j], (unsigned long long)__popc(peers));
+    }
+}
+
 template <bool WARP_PRIVATE>
 __global__ void __launch_bounds__(FLUX_HIST_THREADS)
     flux_hist_kernel(const double *tau, long long n, double scale, const double *edges, int nb,
                      unsigned long long *counts)
 {
     // dynamic shared memory: float edges rounded up [nb + 1], rounded down
-    // [nb + 1], then the histograms
+    // [nb + 1], per warp a queue of 64 pixel indices for the FP64 recheck,
+    // then the histograms
     extern __shared__ __align__(16) unsigned char hraw[];
+    constexpr int NW = FLUX_HIST_THREADS / 32;
     float *eu = reinterpret_cast<float *>(hraw);
     float *ed = eu + (nb + 1);
     const size_t eb = ((size_t)2 * (nb + 1) * sizeof(float) + 15) & ~(size_t)15;
-    unsigned *wh_all = reinterpret_cast<unsigned *>(hraw + eb);
-    unsigned long long *bh = reinterpret_cast<unsigned long long *>(hraw + eb);
-    const int warp = threadIdx.x >> 5, nw = FLUX_HIST_THREADS / 32;
+    long long *queue_all = reinterpret_cast<long long *>(hraw + eb);
+    unsigned char *hist_base = hraw + eb + sizeof(long long) * 64 * NW;
+    unsigned *wh_all = reinterpret_cast<unsigned *>(hist_base);
+    unsigned long long *bh = reinterpret_cast<unsigned long long *>(hist_base);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned *wh = wh_all + (size_t)warp * nb;
+    long long *queue = queue_all + 64 * warp;
     for (int j = threadIdx.x; j <= nb; j += blockDim.x) {
         // float bounds of each edge (no FP64 work per pixel): eu >= e >= ed
         eu[j] = __double2float_ru(edges[j]);
         ed[j] = __double2float_rd(edges[j]);
     }
     if (WARP_PRIVATE) {
-        for (int j = threadIdx.x; j < nb * nw; j += blockDim.x)
+        for (int j = threadIdx.x; j < nb * NW; j += blockDim.x)
             wh_all[j] = 0u;
     } else {
         for (int j = threadIdx.x; j < nb; j += blockDim.x)
@@ -245,9 +263,17 @@ __global__ void __launch_bounds__(FLUX_HIST_THREADS)
     const double norm = nb / (el - e0);
     const float e0f = (float)e0, normf = (float)norm, vmax = (float)(nb - 1);
     const float sf = trunc_to_float(scale);
+    // exp(-scale tau) <= 1 for tau >= 0 and scale >= 0: such a pixel is in the
+    // last bin as soon as it clears that bin's lower edge, when the bins reach 1
+    const bool top_closed = scale >= 0.0 && el >= 1.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double t = tau[i];
+    int qn = 0;   // entries in this warp's recheck queue (warp-uniform)
+    // whole-warp trips: every lane runs the same number of iterations
+    const long long first = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    for (long long base = first; base < n; base += stride) {
+        const long long i = base + lane;
+        const bool valid = i < n;
+        const double t = valid ? tau[i] : 0.0;
         const float y = sf * trunc_to_float(t);
         const float x32 = expf(-y);
         const float rel = fmaf(fabsf(y), 4.8e-7f, 4.8e-7f);
@@ -260,22 +286,38 @@ __global__ void __launch_bounds__(FLUX_HIST_THREADS)
         int j = __float_as_int(v + (12582912.0f - 0.5f)) - 0x4B400000;
         j = j < 0 ? 0 : j;
         // certain: [lo, hi] inside [e_j, e_{j+1}) (the last bin: inside [e_j, e_nb])
-        const bool sure = isfinite(y) && lo >= eu[j] &&
-                          (hi < ed[j + 1] || (j == nb - 1 && hi <= ed[nb]));
-        if (!sure)
-            j = hist_bin64(exp(-scale * t), edges, nb, e0, el, norm);
-        if (j < 0)
-            continue;
-        if (WARP_PRIVATE)
-            atomicAdd(&wh[j], 1u);
-        else
-            atomicAdd(&bh[j], 1ull);
+        const bool last_ok = j == nb - 1 && (hi <= ed[nb] || (top_closed && t >= 0.0));
+        const bool sure = isfinite(y) && lo >= eu[j] && (hi < ed[j + 1] || last_ok);
+        const bool need = valid && !sure;
+        hist_add<WARP_PRIVATE>(valid && sure ? j : -1, wh, bh);
+        // the rest go to the warp's queue, decided 32 at a time by whole warps
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (need)
+            queue[qn + __popc(m & ((1u << lane) - 1u))] = i;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+            const long long k = queue[lane];
+            hist_add<WARP_PRIVATE>(hist_bin64(exp(-scale * tau[k]), edges, nb, e0, el, norm),
+                                   wh, bh);
+            __syncwarp();
+            if (lane < qn - 32)
+                queue[lane] = queue[32 + lane];
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (qn > 0) {
+        const int jj = lane < qn ? hist_bin64(exp(-scale * tau[queue[lane]]), edges, nb, e0, el,
+                                              norm)
+                                 : -1;
+        hist_add<WARP_PRIVATE>(jj, wh, bh);
     }
     __syncthreads();
     if (WARP_PRIVATE) {
         for (int j = threadIdx.x; j < nb; j += blockDim.x) {
             unsigned long long c = 0;
-            for (int w = 0; w < nw; w++)
+            for (int w = 0; w < NW; w++)
                 c += wh_all[(size_t)w * nb + j];
             if (c)
                 atomicAdd(&counts[j], c);
@@ -285,31 +327,6 @@ __global__ void __launch_bounds__(FLUX_HIST_THREADS)
             if (bh[j])
                 atomicAdd(&counts[j], bh[j]);
     }
-}
-
-// dflux = exp(-scale tau) / mean_flux - 1 for `rows` sightlines.
-__global__ void dflux_kernel(const double *tau, long long count, double scale, double inv_mean,
-                             double *out)
-{
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
-        out[i] = exp(-scale * tau[i]) * inv_mean - 1.0;
-}
-
-// power[k] += vmax * sum_rows |F_row(k)|^2 / npix^2, rows in order (one thread per k).
-__global__ void power_accumulate_kernel(const cufftDoubleComplex *F, int rows, int nk, int npix,
-                                        double vmax, double *power)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nk)
-        return;
-    const double inv = 1.0 / ((double)npix * (double)npix);
-    double t = 0.0;
-    for (int r = 0; r < rows; r++) {
-        const cufftDoubleComplex z = F[(size_t)r * nk + k];
-        t += (z.x * z.x + z.y * z.y) * inv;
-    }
-    power[k] += vmax * t;
 }
 
 }  // namespace
@@ -342,8 +359,10 @@ size_t flux_partials(int width) { return (size_t)RED_BLOCKS * width; }
 size_t flux_hist_smem(int nb, bool warp_private)
 {
     const size_t eb = ((size_t)2 * (nb + 1) * sizeof(float) + 15) & ~(size_t)15;
-    return eb + (warp_private ? sizeof(unsigned) * (size_t)nb * (FLUX_HIST_THREADS / 32)
-                              : sizeof(unsigned long long) * (size_t)nb);
+    const size_t queues = sizeof(long long) * 64 * (FLUX_HIST_THREADS / 32);
+    return eb + queues +
+           (warp_private ? sizeof(unsigned) * (size_t)nb * (FLUX_HIST_THREADS / 32)
+                         : sizeof(unsigned long long) * (size_t)nb);
 }
 
 void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
@@ -358,6 +377,8 @@ void launch_flux_hist(const double *tau, long long n, double scale, const double
                                 ((long long)grid * FLUX_HIST_THREADS)) * 32;
     if (nb <= FLUX_WARP_BINS && per_warp < (1ll << 32)) {
         const size_t smem = flux_hist_smem(nb, true);
+        cudaFuncSetAttribute(flux_hist_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
         flux_hist_kernel<true><<<grid, FLUX_HIST_THREADS, smem, s>>>(tau, n, scale, edges, nb,
                                                                      counts);
     } else {
@@ -367,21 +388,6 @@ void launch_flux_hist(const double *tau, long long n, double scale, const double
         flux_hist_kernel<false><<<grid, FLUX_HIST_THREADS, smem, s>>>(tau, n, scale, edges, nb,
                                                                       counts);
     }
-}
-
-void launch_dflux(const double *tau, long long count, double scale, double inv_mean, double *out,
-                  cudaStream_t s)
-{
-    const long long blocks = (count + 255) / 256;
-    dflux_kernel<<<(unsigned)(blocks < 65535 ? (blocks > 0 ? blocks : 1) : 65535), 256, 0, s>>>(
-        tau, count, scale, inv_mean, out);
-}
-
-void launch_power_accumulate(const void *F, int rows, int nk, int npix, double vmax,
-                             double *power, cudaStream_t s)
-{
-    power_accumulate_kernel<<<(nk + 127) / 128, 128, 0, s>>>(
-        (const cufftDoubleComplex *)F, rows, nk, npix, vmax, power);
 }
 
 }  // namespace fsg

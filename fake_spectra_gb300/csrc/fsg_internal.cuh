@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace fsg {
 
@@ -223,11 +225,40 @@ size_t flux_partials(int width);
 // counts[nb] += np.histogram(exp(-scale tau), edges[nb+1]) (device edges)
 void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
                       unsigned long long *counts, cudaStream_t s);
-void launch_dflux(const double *tau, long long count, double scale, double inv_mean, double *out,
-                  cudaStream_t s);
-// power[k] += vmax sum_rows |F(k)|^2 / npix^2 over rows x nk complex (double) F
-void launch_power_accumulate(const void *F, int rows, int nk, int npix, double vmax,
-                             double *power, cudaStream_t s);
+
+// Flux power (fsg_power.cu): own FP64 transforms of sightline pairs.
+// Odd radices up to POWER_MAX_ODD_RADIX run as direct passes; a length with a
+// larger prime factor goes through Bluestein's algorithm.
+constexpr int POWER_MAX_ODD_RADIX = 63;
+struct PowerPass {
+    int radix = 0;
+    long long ns = 1;        // product of the earlier passes' radices
+    long long tw_off = 0;    // table offset of exp(-2 pi i k r / (ns R)), k < ns, r < R
+    long long cs_off = -1;   // odd radix: table offset of (cos, sin)(2 pi t / R), t < R
+};
+struct PowerPlan {
+    long long npix = -1;     // N
+    long long len = 0;       // transform length: N, or Bluestein's M >= 2N - 1
+    bool bluestein = false;
+    std::vector<PowerPass> passes;
+    long long table_len = 0;  // double2 entries of the pass tables
+};
+PowerPlan power_plan(long long npix);
+// Fills the pass tables (table_len entries) and, for Bluestein, the chirp
+// (npix entries) and the transform of the chirp filter (bhat, len entries;
+// scratch: len entries).  Returns the kernel launches.
+int power_plan_tables(const PowerPlan &pl, double2 *tables, double2 *chirp, double2 *bhat,
+                      double2 *scratch, cudaStream_t s);
+// Sightline pairs per chunk: a and b hold pairs x len complex values each.
+long long power_pairs_per_chunk(const PowerPlan &pl, long long nspec);
+// power[k] += vmax / npix^2 * sum over the rows of |rfft(exp(-scale tau) inv_mean - 1)(k)|^2,
+// k = 0 .. npix/2, for `rows` sightlines of tau (DEVICE, rows x npix);
+// partial needs power_partials(npix) doubles.  Returns the kernel launches.
+int power_chunk(const PowerPlan &pl, const double2 *tables, const double2 *chirp,
+                const double2 *bhat, const double *tau, long long rows, double scale,
+                double inv_mean, double vmax, double2 *a, double2 *b, double *partial,
+                double *power, cudaStream_t s);
+size_t power_partials(long long npix);
 
 // After emit: every sightline's cursor must equal its count (DEVERR_PAIR_COUNT
 // otherwise), so no slot of the pair lists is left unwritten.

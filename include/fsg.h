@@ -96,6 +96,7 @@ typedef struct {
     /* host-pointer entry points: the host->device copies of the inputs and the
      * device->host copy of the output of the last call, device time */
     double ms_h2d, ms_d2h;
+    double ms_flux;              /* device time of the last flux-statistics kernel pass */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
@@ -220,7 +221,8 @@ int fsg_mean_flux_device(fsg_context *ctx, const double *tau, int64_t n, double 
 /* The counts of np.histogram(exp(-scale tau), edges) for the flux PDF
  * (fake_spectra/fluxstatistics.py:42-51): bin j holds edges[j] <= F <
  * edges[j+1], the last bin also F == edges[nb]; F outside [edges[0], edges[nb]]
- * or NaN is not counted.  tau DEVICE, edges (nb+1) and counts (nb) HOST. */
+ * or NaN is not counted.  1 <= nb <= 8192.  tau DEVICE, edges (nb+1) and
+ * counts (nb) HOST. */
 int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
                               const double *edges, int nb, int64_t *counts, char *errbuf,
                               size_t errlen);
