@@ -43,6 +43,7 @@ EXPORTS = (
     "fsg_rescale_mean_flux",
     "fsg_mean_flux_scale_device",
     "fsg_mean_flux_device",
+    "fsg_flux_exp_device",
     "fsg_flux_histogram_device",
     "fsg_flux_power_device",
     "fsg_tune_cache_file",
@@ -174,6 +175,7 @@ def load(path=None):
                                                  ctypes.POINTER(_c_d), _p, _c_size]
         L.fsg_mean_flux_device.argtypes = [_p, _p, _c_i64, _c_d, ctypes.POINTER(_c_d), _p,
                                            _c_size]
+        L.fsg_flux_exp_device.argtypes = [_p, _p, _c_i64, _p, _p, _c_size]
         L.fsg_flux_histogram_device.argtypes = [_p, _p, _c_i64, _c_d, _p, _c_int, _p, _p,
                                                 _c_size]
         L.fsg_flux_power_device.argtypes = [_p, _p, _c_i64, _c_i64, _c_d, _c_d, _c_d, _p, _p,

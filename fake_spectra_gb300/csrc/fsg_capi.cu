@@ -92,6 +92,8 @@ struct fsg_context {
     DevBuf flag, tcount, tstart, tsums, idx;                 // _near_lines
     DevBuf fpart, fout, fedges, fcounts, ftau, fdflux, ffft, fpower;   // flux statistics
     DevBuf ptables, pchirp, pbhat, ppart;                    // flux power plan and partials
+    DevBuf fexp;                                             // 2^(j/256) of the flux exponential
+    bool fexp_ready = false;
     PowerPlan pplan;                                         // plan of the last flux power call
     DevBuf vseg, vscratch, vcofm;                            // Voronoi cells
     DevBuf tune_order;                                       // autotuner sample
@@ -159,9 +161,10 @@ struct fsg_context {
                           &line_order, &ticket, &bad, &nbad, &err, &gacc, &counters,
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
-                          &ffft, &fpower, &ptables, &pchirp, &pbhat, &ppart, &vseg, &vscratch,
-                          &vcofm, &tune_order, &prec};
+                          &ffft, &fpower, &ptables, &pchirp, &pbhat, &ppart, &fexp, &vseg,
+                          &vscratch, &vcofm, &tune_order, &prec};
         pplan = PowerPlan{};
+        fexp_ready = false;
         for (DevBuf *b : bufs) {
             if (b->p)
                 cudaFree(b->p);
@@ -383,6 +386,20 @@ long long near_lines(fsg_context *c, const Particles &p, int *out)
     return (long long)last_start + last_count;
 }
 
+// The table of the flux passes' exponential on the device (uploaded once).
+const double *exp_table(fsg_context *c)
+{
+    auto *t = (double *)c->ensure(c->fexp, sizeof(double) * 256);
+    if (!c->fexp_ready) {
+        double h[256];
+        exp_table_host(h);
+        cuda_check(cudaMemcpyAsync(t, h, sizeof h, cudaMemcpyHostToDevice, c->stream), "H2D");
+        cuda_check(cudaStreamSynchronize(c->stream), "exp table");
+        c->fexp_ready = true;
+    }
+    return t;
+}
+
 // get_mean_flux_scale (py_module.cpp:235-260): Newton-Raphson on the scale of
 // tau until the mean of exp(-scale tau) over the pixels with tau <= thresh is
 // mean_flux_desired; the same update and stopping rule.  The scale stays on
@@ -394,13 +411,14 @@ double mean_flux_scale(fsg_context *c, const double *tau, long long n, double mf
                        double thresh)
 {
     cudaStream_t s = c->stream;
+    const double *etab = exp_table(c);
     auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
     auto *state = (double *)c->ensure(c->fout, sizeof(double) * 4);
     const double init[4] = {1.0, 1.0, 0.0, 0.0};
     cuda_check(cudaMemcpyAsync(state, init, sizeof init, cudaMemcpyHostToDevice, s), "H2D");
     double h[4] = {0, 0, 0, 0};
     for (;;) {
-        launch_newton_passes(tau, n, mfd, tol, thresh, NEWTON_BATCH, part, state, s);
+        launch_newton_passes(tau, n, mfd, tol, thresh, NEWTON_BATCH, etab, part, state, s);
         c->stats.gpu_launches += 2 * NEWTON_BATCH;
         cuda_check(cudaGetLastError(), "flux moments launch");
         cuda_check(cudaMemcpyAsync(h, state, sizeof h, cudaMemcpyDeviceToHost, s), "read");
@@ -415,9 +433,10 @@ double mean_flux_scale(fsg_context *c, const double *tau, long long n, double mf
 double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale)
 {
     cudaStream_t s = c->stream;
+    const double *etab = exp_table(c);
     auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
     auto *out = (double *)c->ensure(c->fout, sizeof(double) * 4);
-    launch_flux_sum(tau, n, scale, part, out, s);
+    launch_flux_sum(tau, n, scale, etab, part, out, s);
     c->stats.gpu_launches += 2;
     cuda_check(cudaGetLastError(), "flux sum launch");
     double h = 0.0;
@@ -1663,6 +1682,28 @@ int fsg_mean_flux_device(fsg_context *ctx, const double *tau, int64_t n, double 
     }
 }
 
+int fsg_flux_exp_device(fsg_context *ctx, const double *y, int64_t n, double *out, char *errbuf,
+                        size_t errlen)
+{
+    try {
+        if (!ctx || (n > 0 && (!y || !out)))
+            fail(FSG_ERR_VALUE, "ctx, y and out must not be NULL");
+        if (n < 0)
+            fail(FSG_ERR_VALUE, "n must be >= 0 (got %lld)", (long long)n);
+        cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
+        const double *etab = exp_table(ctx);
+        if (n > 0) {
+            launch_fexp(y, n, etab, out, ctx->stream);
+            ctx->stats.gpu_launches++;
+            cuda_check(cudaGetLastError(), "exp launch");
+        }
+        cuda_check(cudaStreamSynchronize(ctx->stream), "exp");
+        return FSG_OK;
+    } catch (const FsgError &e) {
+        return report(e, errbuf, errlen);
+    }
+}
+
 int fsg_flux_histogram_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
                               const double *edges, int nb, int64_t *counts, char *errbuf,
                               size_t errlen)
@@ -1734,6 +1775,7 @@ int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, in
             cuda_check(cudaStreamSynchronize(s), "flux power tables");
             pl = fresh;
         }
+        const double *etab = exp_table(ctx);
         const long long chunk = power_pairs_per_chunk(pl, nspec);
         const size_t words = sizeof(double2) * (size_t)chunk * (size_t)pl.len;
         auto *a = (double2 *)ctx->ensure(ctx->fdflux, words);
@@ -1746,8 +1788,8 @@ int fsg_flux_power_device(fsg_context *ctx, const double *tau, int64_t nspec, in
             const long long r = (r0 + 2 * chunk <= nspec) ? 2 * chunk : nspec - r0;
             ctx->stats.gpu_launches += power_chunk(
                 pl, (const double2 *)ctx->ptables.p, (const double2 *)ctx->pchirp.p,
-                (const double2 *)ctx->pbhat.p, tau + r0 * npix, r, scale, 1.0 / mean_flux, vmax,
-                a, b, part, dp, s);
+                (const double2 *)ctx->pbhat.p, etab, tau + r0 * npix, r, scale, 1.0 / mean_flux,
+                vmax, a, b, part, dp, s);
             cuda_check(cudaGetLastError(), "flux power launch");
         }
         cuda_check(cudaEventRecord(ctx->ev[3], s), "event");

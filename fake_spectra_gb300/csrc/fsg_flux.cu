@@ -6,6 +6,9 @@
 // Each pass reads tau once.  Sums are deterministic: every block reduces a
 // fixed contiguous range in a fixed order and a second pass adds the block
 // partials in order, so a result does not depend on scheduling.
+#include <cmath>
+
+#include "fsg_fexp.cuh"
 #include "fsg_internal.cuh"
 
 namespace fsg {
@@ -41,35 +44,6 @@ __device__ __forceinline__ void block_range(long long n, long long &lo, long lon
     hi = lo + per < n ? lo + per : n;
 }
 
-// Per block: sum of exp(-scale tau), sum of tau exp(-scale tau) and the count
-// over the pixels with tau <= thresh (py_module.cpp:242-251).
-__global__ void __launch_bounds__(RED_THREADS) flux_moments_kernel(const double *tau, long long n,
-                                                                   double scale, double thresh,
-                                                                   double *part)
-{
-    __shared__ double scratch[RED_THREADS / 32];
-    long long lo, hi;
-    block_range(n, lo, hi);
-    double f = 0.0, tf = 0.0, cnt = 0.0;
-    for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
-        const double t = tau[i];
-        if (t > thresh)
-            continue;
-        const double e = exp(-scale * t);
-        f += e;
-        tf += e * t;
-        cnt += 1.0;
-    }
-    f = block_sum_ordered(f, scratch);
-    tf = block_sum_ordered(tf, scratch);
-    cnt = block_sum_ordered(cnt, scratch);
-    if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = f;
-        part[3 * blockIdx.x + 1] = tf;
-        part[3 * blockIdx.x + 2] = cnt;
-    }
-}
-
 // Newton-Raphson on the device (py_module.cpp:242-258): state[0] = the scale
 // of the last pass, state[1] = the next scale, state[2] = 1 once converged,
 // state[3] = passes.  A pass reads the scale from state[1]; once state[2] is
@@ -77,7 +51,7 @@ __global__ void __launch_bounds__(RED_THREADS) flux_moments_kernel(const double 
 // iterations between reads.
 __global__ void __launch_bounds__(RED_THREADS)
     flux_moments_dev_kernel(const double *tau, long long n, const double *state, double thresh,
-                            double *part)
+                            const double *etab, double *part)
 {
     __shared__ double scratch[RED_THREADS / 32];
     if (state[2] != 0.0)
@@ -85,23 +59,24 @@ __global__ void __launch_bounds__(RED_THREADS)
     const double scale = state[1];
     long long lo, hi;
     block_range(n, lo, hi);
-    double f = 0.0, tf = 0.0, cnt = 0.0;
+    double f = 0.0, tf = 0.0;
+    long long cnt = 0;   // counted in integers: exact, and off the FP64 pipe
     for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
         const double t = tau[i];
         if (t > thresh)
             continue;
-        const double e = exp(-scale * t);
+        const double e = fexp(-scale * t, etab);
         f += e;
-        tf += e * t;
-        cnt += 1.0;
+        tf = fma(e, t, tf);
+        cnt++;
     }
     f = block_sum_ordered(f, scratch);
     tf = block_sum_ordered(tf, scratch);
-    cnt = block_sum_ordered(cnt, scratch);
+    const double cntd = block_sum_ordered((double)cnt, scratch);
     if (threadIdx.x == 0) {
         part[3 * blockIdx.x] = f;
         part[3 * blockIdx.x + 1] = tf;
-        part[3 * blockIdx.x + 2] = cnt;
+        part[3 * blockIdx.x + 2] = cntd;
     }
 }
 
@@ -130,14 +105,15 @@ __global__ void newton_update_kernel(const double *part, int nblocks, double mfd
 
 // Sum of exp(-scale tau) over all pixels (np.mean(np.exp(-tau)) with scale 1).
 __global__ void __launch_bounds__(RED_THREADS) flux_sum_kernel(const double *tau, long long n,
-                                                               double scale, double *part)
+                                                               double scale, const double *etab,
+                                                               double *part)
 {
     __shared__ double scratch[RED_THREADS / 32];
     long long lo, hi;
     block_range(n, lo, hi);
     double f = 0.0;
     for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS)
-        f += exp(-scale * tau[i]);
+        f += fexp(-scale * tau[i], etab);
     f = block_sum_ordered(f, scratch);
     if (threadIdx.x == 0)
         part[blockIdx.x] = f;
@@ -331,27 +307,44 @@ __global__ void __launch_bounds__(FLUX_HIST_THREADS)
 
 }  // namespace
 
-void launch_flux_moments(const double *tau, long long n, double scale, double thresh,
-                         double *part, double *out3, cudaStream_t s)
-{
-    flux_moments_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, scale, thresh, part);
-    partial_sum_kernel<<<1, 32, 0, s>>>(part, RED_BLOCKS, 3, out3);
-}
-
 void launch_newton_passes(const double *tau, long long n, double mfd, double tol, double thresh,
-                          int passes, double *part, double *state, cudaStream_t s)
+                          int passes, const double *etab, double *part, double *state,
+                          cudaStream_t s)
 {
     for (int k = 0; k < passes; k++) {
-        flux_moments_dev_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, state, thresh, part);
+        flux_moments_dev_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, state, thresh, etab,
+                                                                   part);
         newton_update_kernel<<<1, 32, 0, s>>>(part, RED_BLOCKS, mfd, tol, state);
     }
 }
 
-void launch_flux_sum(const double *tau, long long n, double scale, double *part, double *out1,
-                     cudaStream_t s)
+void launch_flux_sum(const double *tau, long long n, double scale, const double *etab,
+                     double *part, double *out1, cudaStream_t s)
 {
-    flux_sum_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, scale, part);
+    flux_sum_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(tau, n, scale, etab, part);
     partial_sum_kernel<<<1, 32, 0, s>>>(part, RED_BLOCKS, 1, out1);
+}
+
+// out[i] = exp(y[i]) as the flux passes evaluate it
+__global__ void fexp_kernel(const double *y, long long n, const double *etab, double *out)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = fexp(y[i], etab);
+}
+
+void launch_fexp(const double *y, long long n, const double *etab, double *out, cudaStream_t s)
+{
+    long long blocks = (n + 255) / 256;
+    blocks = blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks);
+    fexp_kernel<<<(unsigned)blocks, 256, 0, s>>>(y, n, etab, out);
+}
+
+void exp_table_host(double *tab)
+{
+    // 2^(j/256) in extended precision, rounded once to double
+    for (int j = 0; j < 256; j++)
+        tab[j] = (double)std::exp2l((long double)j / 256.0L);
 }
 
 size_t flux_partials(int width) { return (size_t)RED_BLOCKS * width; }

@@ -210,17 +210,20 @@ void launch_voronoi_cells(const float *pos, const int *part, const long long *of
                           cudaStream_t s);
 
 // Flux statistics (fsg_flux.cu): deterministic two-pass reductions over tau.
-// out3 = {sum exp(-scale tau), sum tau exp(-scale tau), count} over tau <= thresh;
-// part needs flux_partials(3) (resp. flux_partials(1)) doubles.
-void launch_flux_moments(const double *tau, long long n, double scale, double thresh,
-                         double *part, double *out3, cudaStream_t s);
-void launch_flux_sum(const double *tau, long long n, double scale, double *part, double *out1,
-                     cudaStream_t s);
+// part needs flux_partials(1) (resp. flux_partials(3)) doubles; etab is the
+// table of exp_table_host on the device (the passes' exponential, fsg_fexp.cuh).
+void launch_flux_sum(const double *tau, long long n, double scale, const double *etab,
+                     double *part, double *out1, cudaStream_t s);
 // `passes` Newton iterations of the mean-flux scale kept on the device:
-// state[4] = {scale of the last pass, next scale (start: 1), converged, passes},
-// part needs flux_partials(3) doubles.  Passes after convergence do nothing.
+// state[4] = {scale of the last pass, next scale (start: 1), converged, passes}.
+// Passes after convergence do nothing.
 void launch_newton_passes(const double *tau, long long n, double mfd, double tol, double thresh,
-                          int passes, double *part, double *state, cudaStream_t s);
+                          int passes, const double *etab, double *part, double *state,
+                          cudaStream_t s);
+// out[i] = exp(y[i]) with the passes' exponential
+void launch_fexp(const double *y, long long n, const double *etab, double *out, cudaStream_t s);
+// tab[256] = 2^(j/256) rounded to double
+void exp_table_host(double *tab);
 size_t flux_partials(int width);
 // counts[nb] += np.histogram(exp(-scale tau), edges[nb+1]) (device edges)
 void launch_flux_hist(const double *tau, long long n, double scale, const double *edges, int nb,
@@ -255,9 +258,9 @@ long long power_pairs_per_chunk(const PowerPlan &pl, long long nspec);
 // k = 0 .. npix/2, for `rows` sightlines of tau (DEVICE, rows x npix);
 // partial needs power_partials(npix) doubles.  Returns the kernel launches.
 int power_chunk(const PowerPlan &pl, const double2 *tables, const double2 *chirp,
-                const double2 *bhat, const double *tau, long long rows, double scale,
-                double inv_mean, double vmax, double2 *a, double2 *b, double *partial,
-                double *power, cudaStream_t s);
+                const double2 *bhat, const double *etab, const double *tau, long long rows,
+                double scale, double inv_mean, double vmax, double2 *a, double2 *b,
+                double *partial, double *power, cudaStream_t s);
 size_t power_partials(long long npix);
 
 // After emit: every sightline's cursor must equal its count (DEVERR_PAIR_COUNT

@@ -28,6 +28,7 @@
 // Memory traffic (one read and one write of 16 bytes per point and pass) is
 // secondary.  Sums over sightlines go in a fixed order: fixed segments of
 // pairs, each summed in order, then the segments in order.
+#include "fsg_fexp.cuh"
 #include "fsg_internal.cuh"
 
 namespace fsg {
@@ -340,7 +341,8 @@ __global__ void chirp_filter_kernel(const double2 *w, unsigned N, unsigned M, do
 // n >= N), d = exp(-scale tau) inv_mean - 1; a missing second row counts as 0.
 __global__ void power_pack_kernel(const double *__restrict__ tau, unsigned rows, unsigned N,
                                   unsigned L, double scale, double inv_mean,
-                                  const double2 *__restrict__ chirp, double2 *__restrict__ z,
+                                  const double2 *__restrict__ chirp,
+                                  const double *__restrict__ etab, double2 *__restrict__ z,
                                   unsigned total)
 {
     const unsigned stride = gridDim.x * blockDim.x;
@@ -349,9 +351,9 @@ __global__ void power_pack_kernel(const double *__restrict__ tau, unsigned rows,
         double2 v = make_double2(0.0, 0.0);
         if (n < N) {
             const size_t ra = 2 * (size_t)p;
-            v.x = exp(-scale * tau[ra * N + n]) * inv_mean - 1.0;
+            v.x = fma(fexp(-scale * tau[ra * N + n], etab), inv_mean, -1.0);
             if (ra + 1 < rows)
-                v.y = exp(-scale * tau[(ra + 1) * N + n]) * inv_mean - 1.0;
+                v.y = fma(fexp(-scale * tau[(ra + 1) * N + n], etab), inv_mean, -1.0);
             if (chirp)
                 v = cmul(v, chirp[n]);
         }
@@ -558,16 +560,17 @@ long long power_pairs_per_chunk(const PowerPlan &pl, long long nspec)
 }
 
 int power_chunk(const PowerPlan &pl, const double2 *tables, const double2 *chirp,
-                const double2 *bhat, const double *tau, long long rows, double scale,
-                double inv_mean, double vmax, double2 *a, double2 *b, double *partial,
-                double *power, cudaStream_t s)
+                const double2 *bhat, const double *etab, const double *tau, long long rows,
+                double scale, double inv_mean, double vmax, double2 *a, double2 *b,
+                double *partial, double *power, cudaStream_t s)
 {
     int launches = 0;
     const unsigned N = (unsigned)pl.npix, L = (unsigned)pl.len;
     const unsigned pairs = (unsigned)((rows + 1) / 2);
     const unsigned total = pairs * L;
     power_pack_kernel<<<grid_for(total, 256), 256, 0, s>>>(
-        tau, (unsigned)rows, N, L, scale, inv_mean, pl.bluestein ? chirp : nullptr, a, total);
+        tau, (unsigned)rows, N, L, scale, inv_mean, pl.bluestein ? chirp : nullptr, etab, a,
+        total);
     launches++;
     double2 *r = run_passes(pl, tables, a, b, pairs, s, launches);
     double norm = 1.0 / ((double)N * (double)N);

@@ -218,6 +218,12 @@ int fsg_mean_flux_scale_device(fsg_context *ctx, const double *tau, int64_t n,
 int fsg_mean_flux_device(fsg_context *ctx, const double *tau, int64_t n, double scale,
                          double *mean, char *errbuf, size_t errlen);
 
+/* out[i] = exp(y[i]) (y, out DEVICE, n doubles) with the FP64 exponential the
+ * mean-flux and flux-power passes use (table-driven, within about one ulp of
+ * exp); exposed so that its accuracy can be checked. */
+int fsg_flux_exp_device(fsg_context *ctx, const double *y, int64_t n, double *out, char *errbuf,
+                        size_t errlen);
+
 /* The counts of np.histogram(exp(-scale tau), edges) for the flux PDF
  * (fake_spectra/fluxstatistics.py:42-51): bin j holds edges[j] <= F <
  * edges[j+1], the last bin also F == edges[nb]; F outside [edges[0], edges[nb]]

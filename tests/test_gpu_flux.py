@@ -172,3 +172,44 @@ def test_flux_histogram_edges_exact(fsg, nb, scale, kind):
 def test_flux_histogram_bin_limit(fsg):
     with pytest.raises(ValueError, match="nbins"):
         _hist_device(np.zeros(10), 1.0, np.arange(8194) / 8193.)
+
+
+def test_flux_exponential_accuracy(fsg):
+    """The table-driven FP64 exponential of the mean-flux and power passes
+    against CUDA's exp and numpy's: within one ulp on the arguments the passes
+    see (-scale tau, from huge to zero) and across the whole double range
+    within two ulps of each (each is itself within about one ulp of the true
+    value), exact at the special values, subnormal results, overflow."""
+    import ctypes
+    import torch
+    from fake_spectra_gb300 import _lib
+    from fake_spectra_gb300 import fluxstatistics as st
+    rng = np.random.default_rng(31)
+    y = np.concatenate([
+        -np.exp(rng.uniform(-40, 7, 2_000_000)),          # -scale tau, tau lognormal-like
+        rng.uniform(-745.2, 709.8, 2_000_000),            # the whole finite range
+        rng.uniform(-1e-3, 1e-3, 200_000), np.linspace(-709, -707, 20001),
+        np.linspace(707, 709.78, 20001), np.linspace(-746, -744, 20001),
+        [0.0, -0.0, 1.0, -1.0, np.log(2.0), 709.78, 709.79, -745.13321910194122, -745.14,
+         -800.0, 1e300, -1e300, np.inf, -np.inf, np.nan, 5e-324, -5e-324]])
+    yd = torch.as_tensor(y, device="cuda")
+    out = torch.empty_like(yd)
+    ctx = st._context()
+    st._bind(ctx)
+    eb = _lib.errbuf()
+    rc = _lib.load().fsg_flux_exp_device(ctx.handle, ctypes.c_void_p(yd.data_ptr()), len(y),
+                                         ctypes.c_void_p(out.data_ptr()), eb, 512)
+    _lib.raise_for(rc, eb.value.decode(errors="replace"))
+    got = out.cpu().numpy()
+    for name, want in (("cuda", torch.exp(yd).cpu().numpy()), ("numpy", np.exp(y))):
+        same_class = (np.isnan(got) == np.isnan(want)) & (np.isinf(got) == np.isinf(want))
+        assert same_class.all(), name
+        fin = np.isfinite(want) & (want > 0)
+        ulps = np.abs(got[fin].view(np.int64) - want[fin].view(np.int64))
+        print("\nflux exp vs %s exp: %.4f%% equal, %.4f%% 1 ulp, max %d ulp" % (
+            name, 100 * np.mean(ulps == 0), 100 * np.mean(ulps == 1), ulps.max()))
+        assert ulps.max() <= 2, (name, int(ulps.max()), y[fin][np.argmax(ulps)])
+        zero = np.isfinite(want) & (want == 0)
+        assert (got[zero] <= 5e-324).all(), name
+    assert got[np.isinf(y) & (y > 0)][0] == np.inf and got[np.isinf(y) & (y < 0)][0] == 0.0
+    assert got[y == 0.0].tolist() == [1.0, 1.0]
