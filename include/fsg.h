@@ -342,9 +342,9 @@ void fsg_tune_cache_clear(void);   /* empties the in-process cache (the file is 
  *   per pixel beside the pair staging area, out of the device's opt-in
  *   maximum less 2 KiB.  With GB300's 227 KiB: 14400 pixels in the FP64 form,
  *   13760 for FP32 optical depths, 14016 for FP32 column densities.
- * The first call on a device looks up the array's address (do it before any
- * stream capture); the address is kept for the life of the process, so a
- * cudaDeviceReset between calls is not supported.  Calls share the array:
+ * The first call on a device looks up the array's address; the address is
+ * kept for the life of the process, so a cudaDeviceReset between calls is not
+ * supported.  Calls share the array:
  * they are serialised by a lock and complete before returning (error returns
  * included); GPU work overlapping a call on the same array would race.
  */
