@@ -121,7 +121,46 @@ def parse_args():
     p.add_argument("--no-bwd", action="store_true")
     p.add_argument("--no-extra", action="store_true",
                    help="skip the multi-channel column density and flux statistics sections")
+    p.add_argument("--flux-only", type=int, default=0, metavar="NSPEC",
+                   help="time only the flux statistics on a seeded synthetic tau of NSPEC x "
+                        "11152 pixels (a small case for profiling their kernels)")
     return p.parse_args()
+
+
+def flux_only(args):
+    """The flux statistics alone on a seeded lognormal tau of nspec x 11152
+    pixels (saturated and empty pixels included), resident on the device."""
+    import torch
+    from fake_spectra_gb300 import build
+    from fake_spectra_gb300 import fluxstatistics as fstat
+    build.build()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2024)
+    nspec, npix = args.flux_only, 11152
+    tau = torch.exp(2.0 * torch.randn((nspec, npix), generator=g, device="cuda",
+                                      dtype=torch.float64))
+    u = torch.rand((nspec, npix), generator=g, device="cuda", dtype=torch.float64)
+    tau[u < 0.01] = 0.0
+    tau[u > 0.99] = 1e4
+    torch.cuda.synchronize()
+    calls = {"mean_flux": lambda: fstat.mean_flux(tau, 0.7),
+             "flux_pdf": lambda: fstat.flux_pdf(tau, 20, None),
+             "flux_power": lambda: fstat.flux_power(tau, npix * 1.0, 8, 0.7, False)}
+    res = {}
+    for name, fn in calls.items():
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        res[name + "_ms"] = (time.perf_counter() - t0) * 1e3 / max(args.steps, 1)
+        res[name + "_kernels_ms"] = fstat._context().stats()["ms_flux"]
+    print(json.dumps({"flux_only": {"nspec": nspec, "npix": npix, "steps": args.steps,
+                                    "warmup": args.warmup, **res,
+                                    "note": "kernels_ms is the device time of the last "
+                                            "call's kernels"}}))
 
 
 def dist_setup():
@@ -500,6 +539,9 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.flux_only:
+        flux_only(args)
         return
     rank, world, local = dist_setup()
     import torch

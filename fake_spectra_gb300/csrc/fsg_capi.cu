@@ -417,12 +417,19 @@ double mean_flux_scale(fsg_context *c, const double *tau, long long n, double mf
     const double init[4] = {1.0, 1.0, 0.0, 0.0};
     cuda_check(cudaMemcpyAsync(state, init, sizeof init, cudaMemcpyHostToDevice, s), "H2D");
     double h[4] = {0, 0, 0, 0};
+    float total = 0.f;
     for (;;) {
+        cuda_check(cudaEventRecord(c->ev[2], s), "event");
         launch_newton_passes(tau, n, mfd, tol, thresh, NEWTON_BATCH, etab, part, state, s);
         c->stats.gpu_launches += 2 * NEWTON_BATCH;
         cuda_check(cudaGetLastError(), "flux moments launch");
+        cuda_check(cudaEventRecord(c->ev[3], s), "event");
         cuda_check(cudaMemcpyAsync(h, state, sizeof h, cudaMemcpyDeviceToHost, s), "read");
         cuda_check(cudaStreamSynchronize(s), "flux moments");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+        total += ms;
+        c->stats.ms_flux = total;
         if (h[2] != 0.0)
             return h[1];
         if (h[3] > 10000)
@@ -436,12 +443,17 @@ double mean_flux_of(fsg_context *c, const double *tau, long long n, double scale
     const double *etab = exp_table(c);
     auto *part = (double *)c->ensure(c->fpart, sizeof(double) * flux_partials(3));
     auto *out = (double *)c->ensure(c->fout, sizeof(double) * 4);
+    cuda_check(cudaEventRecord(c->ev[2], s), "event");
     launch_flux_sum(tau, n, scale, etab, part, out, s);
     c->stats.gpu_launches += 2;
+    cuda_check(cudaEventRecord(c->ev[3], s), "event");
     cuda_check(cudaGetLastError(), "flux sum launch");
     double h = 0.0;
     cuda_check(cudaMemcpyAsync(&h, out, sizeof h, cudaMemcpyDeviceToHost, s), "read");
     cuda_check(cudaStreamSynchronize(s), "flux sum");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    c->stats.ms_flux = ms;
     return h / (double)n;
 }
 

@@ -61,11 +61,21 @@ __global__ void __launch_bounds__(RED_THREADS)
     block_range(n, lo, hi);
     double f = 0.0, tf = 0.0;
     long long cnt = 0;   // counted in integers: exact, and off the FP64 pipe
+    // t > thresh on the bit patterns when thresh has its sign bit clear (the
+    // patterns of non-negative doubles order like the values; NaN compares
+    // false as in FP64), else in FP64
+    const long long thr_bits = __double_as_longlong(thresh);
+    const bool int_cmp = thr_bits >= 0;
+    const double nscale = -scale;
     for (long long i = lo + threadIdx.x; i < hi; i += RED_THREADS) {
         const double t = tau[i];
-        if (t > thresh)
+        const long long tb = __double_as_longlong(t);
+        const bool above = int_cmp ? (tb > thr_bits && (tb & 0x7fffffffffffffffll) <=
+                                                           0x7ff0000000000000ll)
+                                   : t > thresh;
+        if (above)
             continue;
-        const double e = fexp(-scale * t, etab);
+        const double e = fexp(nscale * t, etab);
         f += e;
         tf = fma(e, t, tf);
         cnt++;
@@ -80,18 +90,32 @@ __global__ void __launch_bounds__(RED_THREADS)
     }
 }
 
-// The in-order sums of a pass's block partials and the Newton update (one thread).
+// Fixed-order sum of the `width`-strided block partials' component c by one
+// warp: lane l adds blocks l, l + 32, ... in order, then an xor butterfly
+// (each level adds the same two values in every lane, so all lanes agree).
+__device__ __forceinline__ double warp_partial_sum(const double *part, int nblocks, int width,
+                                                  int c)
+{
+    double t = 0.0;
+    for (int b = threadIdx.x & 31; b < nblocks; b += 32)
+        t += part[(size_t)b * width + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// The fixed-order sums of a pass's block partials and the Newton update (one warp).
 __global__ void newton_update_kernel(const double *part, int nblocks, double mfd, double tol,
                                      double *state)
 {
-    if (threadIdx.x != 0 || state[2] != 0.0)
+    if (state[2] != 0.0)
         return;
-    double f = 0.0, tf = 0.0, cnt = 0.0;
-    for (int b = 0; b < nblocks; b++) {
-        f += part[3 * (size_t)b];
-        tf += part[3 * (size_t)b + 1];
-        cnt += part[3 * (size_t)b + 2];
-    }
+    const double f = warp_partial_sum(part, nblocks, 3, 0);
+    const double tf = warp_partial_sum(part, nblocks, 3, 1);
+    const double cnt = warp_partial_sum(part, nblocks, 3, 2);
+    if (threadIdx.x != 0)
+        return;
     const double scale = state[1];
     double newscale = scale + (f - mfd * cnt) / tf;
     if (newscale <= 0)
@@ -119,16 +143,14 @@ __global__ void __launch_bounds__(RED_THREADS) flux_sum_kernel(const double *tau
         part[blockIdx.x] = f;
 }
 
-// In-order sum of `width`-strided block partials (one thread per component).
+// Fixed-order sums of `width`-strided block partials (one warp).
 __global__ void partial_sum_kernel(const double *part, int nblocks, int width, double *out)
 {
-    const int c = threadIdx.x;
-    if (c >= width)
-        return;
-    double t = 0.0;
-    for (int b = 0; b < nblocks; b++)
-        t += part[(size_t)b * width + c];
-    out[c] = t;
+    for (int c = 0; c < width; c++) {
+        const double t = warp_partial_sum(part, nblocks, width, c);
+        if (threadIdx.x == 0)
+            out[c] = t;
+    }
 }
 
 // np.histogram with explicit edges (numpy's sorted-search rule): bin j holds

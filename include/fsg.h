@@ -96,7 +96,7 @@ typedef struct {
     /* host-pointer entry points: the host->device copies of the inputs and the
      * device->host copy of the output of the last call, device time */
     double ms_h2d, ms_d2h;
-    double ms_flux;              /* device time of the last flux-statistics kernel pass */
+    double ms_flux;              /* device time of the last flux-statistics call's kernels */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
