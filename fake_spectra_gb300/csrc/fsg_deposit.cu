@@ -887,6 +887,28 @@ struct Tau32 {
             }
             return total;
         }
+        // small damping (uniform over the warp: one pair): the first-order form
+        // where every node is inside its table, else per node with the wing
+        // form (the counting variant keeps the forms it counts)
+        if (!COUNT && vc.a <= VOIGT_SMALL_A) {
+            bool in = true;
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                in &= fabsf(u[i]) < VOIGT_SMALL_X;
+            if (__all_sync(0xffffffffu, in)) {
+#pragma unroll
+                for (int i = 0; i < NODES; ++i)
+                    total = fmaf(voigt_small32(u[i], vc), w[i], total);
+                return total;
+            }
+#pragma unroll
+            for (int i = 0; i < NODES; ++i) {
+                const float h = fabsf(u[i]) < VOIGT_SMALL_X ? voigt_small32(u[i], vc)
+                                                            : voigt_wing32(u[i], vc);
+                total = fmaf(h, w[i], total);
+            }
+            return total;
+        }
         if (__all_sync(0xffffffffu, core)) {
 #pragma unroll
             for (int i = 0; i < NODES; ++i)

@@ -245,6 +245,34 @@ __device__ __forceinline__ float voigt_core32(float u, const Voigt32 &c, const f
     return fmaf(-c.two_a_sqpi, br, gauss);
 }
 
+// Small-damping form (a <= VOIGT_SMALL_A, |u| < 15.9): to first order in a,
+//   H = exp(-x^2) (1 + a^2 (1 - 2 x^2)) + a K(x),  K = -(2/sqrt(pi)) (1 - 2 x F(x)),
+// from the expansion w(x + i a) = w(x) + i a w'(x) - a^2 w''(x)/2 + O(a^3) with
+// w' = -2 z w + 2i/sqrt(pi); the dropped terms are below 6e-7 of H for
+// a <= 2e-3 (checked against scipy's wofz).  K does not depend on a: one cubic
+// per interval of 0.1 (voigt_table.h, read through L1) gives it within 2.3e-7
+// of H.  About 17 instructions a node against about 47 for the core form.
+constexpr float VOIGT_SMALL_A = 2e-3f;
+constexpr float VOIGT_SMALL_X = 15.9f;   // the table covers [0, 16)
+
+__device__ const float4 d_ktab[FSG_KTAB_N] = FSG_KTAB_INIT;
+
+__device__ __forceinline__ float voigt_small32(float u, const Voigt32 &c)
+{
+    const float x = fabsf(u);
+    const float x2 = x * x;
+    // interval j = floor(10 x) (a tie at an integer may give j - 1 with t = 1,
+    // the same value by continuity) without int<->float conversions
+    const float m = fmaf(x, 10.0f, 12582912.0f - 0.5f);
+    const int j = __float_as_int(m) - 0x4B400000;
+    const float t = fmaf(x, 10.0f, -(m - 12582912.0f));
+    const float4 k = __ldg(&d_ktab[j]);
+    const float kx = fmaf(fmaf(fmaf(k.w, t, k.z), t, k.y), t, k.x);
+    const float e = __expf(-x2);
+    const float g = fmaf(c.a2, fmaf(-2.0f, x2, 1.0f), 1.0f);
+    return fmaf(e, g, c.a * kx);
+}
+
 template <bool COUNT>
 __device__ __forceinline__ float voigt_f32(float u, const Voigt32 &c, const float2 *tab,
                                            unsigned &n_near)
