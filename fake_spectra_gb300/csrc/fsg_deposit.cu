@@ -1293,6 +1293,31 @@ __device__ __forceinline__ void accumulate(unsigned *dev_err, R v, int j, int S,
                                            unsigned long long *lo, unsigned long long *hi,
                                            int *bad)
 {
+    if constexpr (FMT == 1 && std::is_same<R, float>::value) {
+        // Non-negative finite v with v 2^S = m 2^p, 0 <= p <= 68 (every optical
+        // depth contribution: the bound puts the sightline total at 2^91, and a
+        // walk stops long before 2^-68 of it): the split_from result without
+        // branches.  c = m << min(p, 40) fits in 64 bits (m < 2^24); its low
+        // word is lo (zero once p >= 32) and its high word, shifted on by the
+        // rest of p, is hi.  Everything else takes the general path below.
+        const unsigned fb = __float_as_uint(v);
+        if (fb < 0x7F800000u) {
+            const unsigned e8 = fb >> 23;
+            const unsigned m = (fb & 0x7FFFFFu) | (e8 ? 0x800000u : 0u);
+            const int p = (int)(e8 ? e8 : 1u) - 150 + S;
+            if ((unsigned)p <= 68u) {
+                const int ps = min(p, 40);
+                const unsigned long long c = (unsigned long long)m << ps;
+                const unsigned l32 = (unsigned)c;
+                const unsigned long long h = (c >> 32) << (p - ps);
+                if (l32)
+                    atomicAdd(&lo[j], (unsigned long long)l32);
+                if (h)
+                    atomicAdd(&hi[j], h);
+                return;
+            }
+        }
+    }
     if (!isfinite(v)) {
         *bad = 1;
         return;
