@@ -870,6 +870,53 @@ struct Tau32 {
     {
         float total = 0.f;
         float u[NODES];
+        if constexpr (!COUNT) {
+            // The node offsets are (i - 3) u1: max_i |U_i - V| = |V| + |U_6|
+            // exactly (the same float sum as the farther end node's), and
+            // |V| - |U_6| is min_i |U_i - V| once |V| >= |U_6| (a lower bound
+            // otherwise).  Three tests instead of three per node.
+            const float av = fabsf(V), ext = fabsf(U[NODES - 1]);
+            const float near = av - ext, far = av + ext;
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                u[i] = U[i] - V;
+            if (__all_sync(0xffffffffu, near >= 6.5f)) {
+#pragma unroll
+                for (int i = 0; i < NODES; ++i)
+                    total = fmaf(voigt_wing32(u[i], vc), w[i], total);
+                return total;
+            }
+            // small damping (uniform over the warp: one pair): the first-order
+            // form where every node is inside its table, else per node with
+            // the wing form
+            if (vc.a <= VOIGT_SMALL_A) {
+                if (__all_sync(0xffffffffu, far < VOIGT_SMALL_X)) {
+#pragma unroll
+                    for (int i = 0; i < NODES; ++i)
+                        total = fmaf(voigt_small32(u[i], vc), w[i], total);
+                    return total;
+                }
+#pragma unroll
+                for (int i = 0; i < NODES; ++i) {
+                    const float h = fabsf(u[i]) < VOIGT_SMALL_X ? voigt_small32(u[i], vc)
+                                                                : voigt_wing32(u[i], vc);
+                    total = fmaf(h, w[i], total);
+                }
+                return total;
+            }
+            if (__all_sync(0xffffffffu, far < 11.9f)) {   // the core form's table ends at 12
+#pragma unroll
+                for (int i = 0; i < NODES; ++i)
+                    total = fmaf(voigt_core32(u[i], vc, tab), w[i], total);
+                return total;
+            }
+            unsigned nn = 0;
+#pragma unroll
+            for (int i = 0; i < NODES; ++i)
+                total = fmaf(voigt_f32<COUNT>(u[i], vc, tab, nn), w[i], total);
+            return total;
+        }
+        // the counting variant: the per-node tests whose paths it counts
         bool wing = true, core = true;
 #pragma unroll
         for (int i = 0; i < NODES; ++i) {
@@ -884,28 +931,6 @@ struct Tau32 {
             if (COUNT) {
                 ct.b += NODES;
                 ct.e++;
-            }
-            return total;
-        }
-        // small damping (uniform over the warp: one pair): the first-order form
-        // where every node is inside its table, else per node with the wing
-        // form (the counting variant keeps the forms it counts)
-        if (!COUNT && vc.a <= VOIGT_SMALL_A) {
-            bool in = true;
-#pragma unroll
-            for (int i = 0; i < NODES; ++i)
-                in &= fabsf(u[i]) < VOIGT_SMALL_X;
-            if (__all_sync(0xffffffffu, in)) {
-#pragma unroll
-                for (int i = 0; i < NODES; ++i)
-                    total = fmaf(voigt_small32(u[i], vc), w[i], total);
-                return total;
-            }
-#pragma unroll
-            for (int i = 0; i < NODES; ++i) {
-                const float h = fabsf(u[i]) < VOIGT_SMALL_X ? voigt_small32(u[i], vc)
-                                                            : voigt_wing32(u[i], vc);
-                total = fmaf(h, w[i], total);
             }
             return total;
         }
