@@ -21,6 +21,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <condition_variable>
 #include <mutex>
 #include <thread>
 #include <numeric>
@@ -106,6 +107,12 @@ struct fsg_context {
     // inputs, up[1] orders the deposit after them
     cudaStream_t side = nullptr;
     cudaEvent_t up[2] = {nullptr, nullptr};
+    // host-pointer entry: row groups of the deposit (their order, the event
+    // after each group's launch, the event after each group's output copy)
+    static constexpr int ROW_GROUPS = 4;
+    DevBuf gorder;
+    cudaEvent_t gdone[ROW_GROUPS] = {}, gcopied[ROW_GROUPS] = {};
+    std::vector<int> h_bad;   // sightlines the FP64 fallback redid in the last deposit
     // host mirrors
     std::vector<long long> h_off;
     std::vector<int> h_order;
@@ -162,7 +169,7 @@ struct fsg_context {
                           &skey, &sperm, &shist, &sstart, &ssums, &flag, &tcount, &tstart,
                           &tsums, &idx, &fpart, &fout, &fedges, &fcounts, &ftau, &fdflux,
                           &ffft, &fpower, &ptables, &pchirp, &pbhat, &ppart, &fexp, &vseg,
-                          &vscratch, &vcofm, &tune_order, &prec};
+                          &vscratch, &vcofm, &tune_order, &prec, &gorder};
         pplan = PowerPlan{};
         fexp_ready = false;
         for (DevBuf *b : bufs) {
@@ -462,8 +469,19 @@ void apply_tuning(fsg_context *c, const LineParams &lp, const fsg_options *opt, 
                   PairLists pl, double *out, DepositLaunch &cfg);
 
 // 3. deposit into out (device, nlos*nbins)
+// Row groups of a deposit: the sightlines in `groups` contiguous index
+// ranges, launched one range after another (each range in the descending
+// pair-count order); on_group(g, row0, row1) runs after range g is queued,
+// with c->gdone[g] recorded behind it.  The output is the same: the
+// fixed-point sums do not depend on the launch.
+struct RowGroups {
+    int groups = 1;
+    std::function<void(int, long long, long long)> on_group;
+};
+
 void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *out,
-             const fsg_options *opt, const float2 *seg = nullptr)
+             const fsg_options *opt, const float2 *seg = nullptr,
+             const RowGroups *rows = nullptr)
 {
     cudaStream_t s = c->stream;
     const int nlos = c->nlos;
@@ -496,25 +514,61 @@ void deposit(fsg_context *c, const LineParams &lp, const Particles &p, double *o
         ctr = (unsigned long long *)c->ensure(c->counters, sizeof(unsigned long long) * 8);
         cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long) * 8, s), "memset");
     }
-    auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned));
+    const int G = (rows && rows->groups > 1 && !count && nlos >= 64 * rows->groups)
+                      ? std::min(rows->groups, (int)fsg_context::ROW_GROUPS)
+                      : 1;
+    auto *ticket = (unsigned *)c->ensure(c->ticket, sizeof(unsigned) * G);
     auto *bad = (int *)c->ensure(c->bad, sizeof(int) * nlos);
     auto *nbad = (int *)c->ensure(c->nbad, sizeof(int));
     auto *err = (unsigned *)c->ensure(c->err, sizeof(unsigned));
-    cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s), "memset");
+    cuda_check(cudaMemsetAsync(ticket, 0, sizeof(unsigned) * G, s), "memset");
     cuda_check(cudaMemsetAsync(nbad, 0, sizeof(int), s), "memset");
     cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), s), "memset");
-    c->stats.gpu_launches += launch_deposit(lp, c->tables, p, pl, (const int *)c->line_order.p,
-                                            nlos, out, ticket, bad, nbad, err, gacc, ctr, cfg, s);
-    cuda_check(cudaGetLastError(), "deposit launch");
+    if (G == 1) {
+        c->stats.gpu_launches += launch_deposit(lp, c->tables, p, pl,
+                                                (const int *)c->line_order.p, nlos, out, ticket,
+                                                bad, nbad, err, gacc, ctr, cfg, s);
+        cuda_check(cudaGetLastError(), "deposit launch");
+    } else {
+        // group g: rows [nlos g / G, nlos (g + 1) / G), in the global order
+        std::vector<int> gord((size_t)nlos);
+        std::vector<long long> start((size_t)G + 1, 0);
+        const auto group_of = [&](int line) { return (int)((long long)line * G / nlos); };
+        for (int line : c->h_order)
+            start[group_of(line) + 1]++;
+        for (int g = 0; g < G; g++)
+            start[g + 1] += start[g];
+        std::vector<long long> fill(start.begin(), start.end() - 1);
+        for (int line : c->h_order)
+            gord[(size_t)fill[group_of(line)]++] = line;
+        auto *dord = (int *)c->ensure(c->gorder, sizeof(int) * (size_t)nlos);
+        cuda_check(cudaMemcpyAsync(dord, gord.data(), sizeof(int) * (size_t)nlos,
+                                   cudaMemcpyHostToDevice, s), "upload order");
+        // the host vector must outlive the copy
+        cuda_check(cudaStreamSynchronize(s), "upload order");
+        for (int g = 0; g < G; g++) {
+            c->stats.gpu_launches += launch_deposit(
+                lp, c->tables, p, pl, dord + start[g], (int)(start[g + 1] - start[g]), out,
+                ticket + g, bad, nbad, err, gacc, ctr, cfg, s);
+            cuda_check(cudaGetLastError(), "deposit launch");
+            cuda_check(cudaEventRecord(c->gdone[g], s), "event");
+            if (rows->on_group)
+                rows->on_group(g, (long long)nlos * g / G, (long long)nlos * (g + 1) / G);
+        }
+    }
     int h_nbad = 0;
     unsigned h_err = 0;
     cuda_check(cudaMemcpyAsync(&h_nbad, nbad, sizeof(int), cudaMemcpyDeviceToHost, s), "read");
     cuda_check(cudaMemcpyAsync(&h_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read");
     cuda_check(cudaStreamSynchronize(s), "deposit");
+    c->h_bad.clear();
     if (h_nbad > 0) {
         launch_deposit_fallback(lp, c->tables, p, pl, bad, h_nbad, out, err, s);
         c->stats.gpu_launches++;
         cuda_check(cudaGetLastError(), "fallback launch");
+        c->h_bad.resize((size_t)h_nbad);
+        cuda_check(cudaMemcpyAsync(c->h_bad.data(), bad, sizeof(int) * (size_t)h_nbad,
+                                   cudaMemcpyDeviceToHost, s), "read");
     }
     c->stats.fallback_lines = h_nbad;
     cuda_check(cudaEventRecord(c->ev[3], s), "event");
@@ -986,6 +1040,10 @@ void ctx_init(fsg_context *c, int device)
     cuda_check(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "cudaStreamCreate");
     for (auto &e : c->up)
         cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    for (auto &e : c->gdone)
+        cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    for (auto &e : c->gcopied)
+        cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
 }
 
 // Copies n bytes between host buffers with up to `threads` threads (pieces
@@ -1125,7 +1183,8 @@ void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, dou
                      double velfac, double lambda, double gamma, double fosc, double amumass,
                      double tautail, const Particles &p, const int32_t *axis, const double *cofm,
                      int32_t nlos, double *out, const fsg_options *opt,
-                     const std::function<void()> &before_deposit = nullptr)
+                     const std::function<void()> &before_deposit = nullptr,
+                     const RowGroups *rows = nullptr)
 {
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
     build_tables(c, axis, cofm, nlos, box);
@@ -1136,7 +1195,7 @@ void run_interpolate(fsg_context *c, int compute_tau, int nbins, int kernel, dou
     LineParams lp = make_line_params(compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc,
                                      amumass, tautail);
     const float2 *seg = kernel == VORONOI ? voronoi_cells(c, p, cofm, box) : nullptr;
-    deposit(c, lp, p, out, opt, seg);
+    deposit(c, lp, p, out, opt, seg, rows);
 }
 
 }  // namespace
@@ -1198,6 +1257,12 @@ void fsg_context_destroy(fsg_context *ctx)
         if (e)
             cudaEventDestroy(e);
     for (auto &e : ctx->up)
+        if (e)
+            cudaEventDestroy(e);
+    for (auto &e : ctx->gdone)
+        if (e)
+            cudaEventDestroy(e);
+    for (auto &e : ctx->gcopied)
         if (e)
             cudaEventDestroy(e);
     if (ctx->side) {
@@ -1291,19 +1356,35 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         // the helper thread stages what only the deposit reads while the search runs;
         // it is joined on every path, and no copy of the caller's arrays outlives
         // the call (error returns included)
-        std::thread helper;
+        std::thread helper, drain;
         std::string helper_err;
+        // output rows copied so far by row group (the drain thread copies group
+        // g into the caller's array once its device-to-staging copy is done)
+        std::mutex gmu;
+        std::condition_variable gcv;
+        int queued = 0;          // groups whose copies are queued
+        bool abandon = false;    // error path: the drain thread stops
         struct Guard {
             fsg_context *c;
-            std::thread &t;
+            std::thread &t, &d;
+            std::mutex &mu;
+            std::condition_variable &cv;
+            bool &abandon;
             ~Guard()
             {
+                {
+                    std::lock_guard<std::mutex> l(mu);
+                    abandon = true;
+                }
+                cv.notify_all();
                 if (t.joinable())
                     t.join();
+                if (d.joinable())
+                    d.join();
                 cudaStreamSynchronize(c->side);
                 cudaStreamSynchronize(c->stream);
             }
-        } guard{c, helper};
+        } guard{c, helper, drain, gmu, gcv, abandon};
         Particles p;
         p.n = npart;
         auto *dpos = (float *)c->ensure(c->pos, n3);
@@ -1358,16 +1439,83 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
             cuda_check(cudaStreamWaitEvent(s, c->up[1], 0), "wait for uploads");
         };
         double *dout = (double *)c->ensure(c->out, nout);
+        // the output leaves in row groups: group g's rows go to the staging
+        // area on the side stream once its deposit launch is done, and the
+        // drain thread moves them into the caller's array while later groups
+        // compute
+        std::vector<long long> grow0(fsg_context::ROW_GROUPS), grow1(fsg_context::ROW_GROUPS);
+        RowGroups rg;
+        rg.groups = fsg_context::ROW_GROUPS;
+        rg.on_group = [&](int g, long long r0, long long r1) {
+            const size_t b0 = sizeof(double) * (size_t)r0 * nbins;
+            const size_t nb = sizeof(double) * (size_t)(r1 - r0) * nbins;
+            cuda_check(cudaStreamWaitEvent(c->side, c->gdone[g], 0), "wait for rows");
+            if (nb)
+                cuda_check(cudaMemcpyAsync(hs + o_out + b0, (char *)dout + b0, nb,
+                                           cudaMemcpyDeviceToHost, c->side), "D2H");
+            cuda_check(cudaEventRecord(c->gcopied[g], c->side), "event");
+            grow0[g] = r0;
+            grow1[g] = r1;
+            {
+                std::lock_guard<std::mutex> l(gmu);
+                queued = g + 1;
+            }
+            gcv.notify_all();
+        };
+        std::string drain_err;
+        drain = std::thread([&] {
+            if (cudaSetDevice(c->device) != cudaSuccess)
+                return;
+            for (int g = 0; g < fsg_context::ROW_GROUPS; g++) {
+                {
+                    std::unique_lock<std::mutex> l(gmu);
+                    gcv.wait(l, [&] { return queued > g || abandon; });
+                    if (queued <= g)
+                        return;
+                }
+                const cudaError_t e = cudaEventSynchronize(c->gcopied[g]);
+                if (e != cudaSuccess) {
+                    drain_err = cudaGetErrorString(e);
+                    return;
+                }
+                const size_t b0 = sizeof(double) * (size_t)grow0[g] * nbins;
+                parallel_copy((char *)out + b0, hs + o_out + b0,
+                              sizeof(double) * (size_t)(grow1[g] - grow0[g]) * nbins, nthr);
+            }
+        });
         run_interpolate(c, compute_tau, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
-                        tautail, p, axis, cofm, nlos, dout, opt, inputs_ready);
+                        tautail, p, axis, cofm, nlos, dout, opt, inputs_ready, &rg);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->cp[0], c->cp[1]);
         c->stats.ms_h2d = ms;   // first staging copy to the last upload (search overlapped)
         const auto t0 = std::chrono::steady_clock::now();
-        if (nout)
-            cuda_check(cudaMemcpyAsync(hs + o_out, dout, nout, cudaMemcpyDeviceToHost, s), "D2H");
-        cuda_check(cudaStreamSynchronize(s), "D2H");
-        parallel_copy(out, hs + o_out, nout, nthr);
+        if (queued == 0) {
+            // one launch (few sightlines, or nothing to deposit): copy it all
+            {
+                std::lock_guard<std::mutex> l(gmu);
+                abandon = true;
+            }
+            gcv.notify_all();
+            drain.join();
+            if (nout)
+                cuda_check(cudaMemcpyAsync(hs + o_out, dout, nout, cudaMemcpyDeviceToHost, s),
+                           "D2H");
+            cuda_check(cudaStreamSynchronize(s), "D2H");
+            parallel_copy(out, hs + o_out, nout, nthr);
+        } else {
+            drain.join();
+            if (!drain_err.empty())
+                fail(FSG_ERR_CUDA, "output copy: %s", drain_err.c_str());
+            // rows the FP64 fallback redid after their group was copied
+            for (int line : c->h_bad) {
+                const size_t b0 = sizeof(double) * (size_t)line * nbins;
+                const size_t nb = sizeof(double) * (size_t)nbins;
+                cuda_check(cudaMemcpyAsync(hs + o_out + b0, (char *)dout + b0, nb,
+                                           cudaMemcpyDeviceToHost, s), "D2H");
+                cuda_check(cudaStreamSynchronize(s), "D2H");
+                memcpy((char *)out + b0, hs + o_out + b0, nb);
+            }
+        }
         c->stats.ms_d2h =
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
                 .count();   // device-to-staging copy and the copy into the caller's array
