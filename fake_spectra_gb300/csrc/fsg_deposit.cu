@@ -2307,6 +2307,22 @@ struct GradSums {
 __device__ __forceinline__ GradSums grad_node_sums(const Tau32 &s, float V, const float2 *tab)
 {
     GradSums g = {0.f, 0.f, 0.f};
+    // the small-damping form when every node of every lane is inside its table
+    // (max_i |U_i - V| = |V| + |U_6|; uniform over the warp)
+    const bool small =
+        s.vc.a <= VOIGT_SMALL_A &&
+        __all_sync(0xffffffffu, fabsf(V) + fabsf(s.U[NODES - 1]) < VOIGT_SMALL_X);
+    if (small) {
+#pragma unroll
+        for (int i = 0; i < NODES; ++i) {
+            const float u = s.U[i] - V;
+            const VoigtGrad r = voigt_grad_small32(u, s.vc);
+            g.d = fmaf(s.w[i], r.h, g.d);
+            g.v = fmaf(s.w[i], r.hu, g.v);
+            g.t = fmaf(s.w[i], r.h + fmaf(u, r.hu, s.aa_f * r.ha), g.t);
+        }
+        return g;
+    }
 #pragma unroll
     for (int i = 0; i < NODES; ++i) {
         const float u = s.U[i] - V;

@@ -348,6 +348,31 @@ struct VoigtGrad {
     float h, hu, ha;
 };
 
+// The small-damping form (voigt_small32) with its derivatives:
+//   dH/dx = -2 x exp(-x^2) (1 + a^2 (1 - 2 x^2) + 2 a^2) + a K'(x),
+//   dH/da = 2 a (1 - 2 x^2) exp(-x^2) + K(x),
+// K' from the derivative of the interval's cubic.
+__device__ __forceinline__ VoigtGrad voigt_grad_small32(float u, const Voigt32 &c)
+{
+    VoigtGrad r;
+    const float x = fabsf(u);
+    const float x2 = x * x;
+    const float m = fmaf(x, 10.0f, 12582912.0f - 0.5f);
+    const int j = __float_as_int(m) - 0x4B400000;
+    const float t = fmaf(x, 10.0f, -(m - 12582912.0f));
+    const float4 k = __ldg(&d_ktab[j]);
+    const float kx = fmaf(fmaf(fmaf(k.w, t, k.z), t, k.y), t, k.x);
+    const float dk = 10.0f * fmaf(fmaf(3.0f * k.w, t, 2.0f * k.z), t, k.y);
+    const float e = __expf(-x2);
+    const float q = fmaf(-2.0f, x2, 1.0f);
+    const float g = fmaf(c.a2, q, 1.0f);
+    r.h = fmaf(e, g, c.a * kx);
+    const float dhdx = fmaf(-2.0f * x * e, fmaf(2.0f, c.a2, g), c.a * dk);
+    r.hu = u < 0.0f ? -dhdx : dhdx;
+    r.ha = fmaf(2.0f * c.a * e, q, kx);
+    return r;
+}
+
 __device__ __forceinline__ VoigtGrad voigt_grad32(float u, const Voigt32 &c, const float2 *tab)
 {
     VoigtGrad r;
