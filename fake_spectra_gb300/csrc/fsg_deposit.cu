@@ -1473,8 +1473,9 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
 // sums, which is linear in the node values and so equals the sum over pairs of
 // each pair's interpolant.  The far wing is a polynomial in 1/V^2 (pole at
 // V = 0), so with the tile half-width at most 0.2 of the distance to the pole
-// the interpolation error of 10 Chebyshev nodes is below 1e-7 of the value
-// (1/V^2: 3e-9, 1/V^4: 1e-7 times its share, which is small that far out).
+// the interpolation error of 8 Chebyshev nodes is below 5e-7 of the value
+// (1/V^2: 2.3e-7, 1/V^4: 6.2e-6 times its share, at most a few percent that
+// far out; 10 nodes gave 3e-9 for 2.7% more deposit time).
 // The window rule needs no per-pixel test inside such a tile: the far wing
 // decreases with |V| (STAGE_TILES), and its value equals tautail at a radius
 // V_stop found once per pair by Newton's method on the multipole polynomial;
@@ -1485,7 +1486,7 @@ __device__ __noinline__ void walk_tau_careful(const DepositArgs &a, const PairIn
 // walked pixel by pixel as before.  The (tile, node) items of a run of tiles
 // are spread over the 32 lanes.
 constexpr int TILE_W = 64;
-constexpr int TILE_M = 10;
+constexpr int TILE_M = 8;
 constexpr float TILE_DIST = 128.f;
 
 __device__ double g_tile_w[TILE_W * TILE_M];   // [pixel in tile][node] interpolation weights

@@ -4,7 +4,7 @@
   float cell range covers every cell the double range covered: a C
   restatement of those formulas (tests/search_bounds.c) on seeded adversarial
   cases (thin shell |dr| ~ hh, periodic edges, six box sizes).
-* The far-field tiles' interpolation error: 10 Chebyshev nodes on a tile whose
+* The far-field tiles' interpolation error: 8 Chebyshev nodes on a tile whose
   half-width is at most 0.2 of the distance to the pole of the 1/V^(2r) wing
   terms.
 """
@@ -45,5 +45,5 @@ def _cheb_rel_err(t, m, n):
 def test_tile_interpolation_error():
     # tile half-width 32 pixels, nearest pixel edge >= 128 pixels from the line centre
     t = 32.0 / (128.0 + 32.0)
-    assert _cheb_rel_err(t, 10, 2) < 1e-8     # the dominant 1/V^2 term
-    assert _cheb_rel_err(t, 10, 4) < 2e-7     # 1/V^4, a small share of the wing
+    assert _cheb_rel_err(t, 8, 2) < 3e-7      # the dominant 1/V^2 term
+    assert _cheb_rel_err(t, 8, 4) < 7e-6      # 1/V^4, a few percent of the wing there
