@@ -1397,13 +1397,21 @@ int fsg_particle_interpolate(int compute_tau, int nbins, int kernel, double box,
         p.dens = ddens;
         p.vel = dvel;
         p.temp = dtemp;
-        // the search reads pos and h: staged and sent first
+        // the search reads pos and h: staged and sent first, in pieces, so
+        // that each piece's upload overlaps the staging of the next
         cuda_check(cudaEventRecord(c->cp[0], s), "event");
-        parallel_copy(hs, pos, n3, nthr);
-        parallel_copy(hs + o_h, h, n1, nthr);
+        const auto stage_up = [&](void *dst, const void *src, size_t off, size_t n) {
+            const size_t piece = (size_t)256 << 20;
+            for (size_t b = 0; b < n; b += piece) {
+                const size_t len = std::min(piece, n - b);
+                parallel_copy(hs + off + b, (const char *)src + b, len, nthr);
+                cuda_check(cudaMemcpyAsync((char *)dst + b, hs + off + b, len,
+                                           cudaMemcpyHostToDevice, s), "H2D");
+            }
+        };
         if (npart > 0) {
-            cuda_check(cudaMemcpyAsync(dpos, hs, n3, cudaMemcpyHostToDevice, s), "H2D");
-            cuda_check(cudaMemcpyAsync(dh, hs + o_h, n1, cudaMemcpyHostToDevice, s), "H2D");
+            stage_up(dpos, pos, 0, n3);
+            stage_up(dh, h, o_h, n1);
         }
         helper = std::thread([&] {
             const cudaError_t e0 = cudaSetDevice(c->device);
