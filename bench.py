@@ -54,11 +54,11 @@ F_EVAL = 32
 FLOPS_FP32 = {"core": 69, "wing": 32, "other": 214, "multipole": 20.0 / 7.0}
 # DRAM traffic of the FP32 deposit from one ncu capture of the 512^3 workload's
 # recipe at 192^3 particles and 2048 sightlines (dram__bytes_read.sum +
-# dram__bytes_write.sum, kept with the profile summaries): 2.372797 GB read for
-# 5038719 pairs, 0.174416896 GB written for 2048 x 11152 pixels; scaled to a
+# dram__bytes_write.sum, kept with the profile summaries): 2.751220 GB read for
+# 5038719 pairs, 0.245783040 GB written for 2048 x 11152 pixels; scaled to a
 # launch by pairs (reads) and output pixels (writes).
-TRAFFIC_READ_PER_PAIR = 2.372797e9 / 5038719
-TRAFFIC_WRITE_PER_PIXEL = 0.174416896e9 / (2048 * 11152)
+TRAFFIC_READ_PER_PAIR = 2.751220e9 / 5038719
+TRAFFIC_WRITE_PER_PIXEL = 0.245783040e9 / (2048 * 11152)
 FLOPS_FP64 = {"core": 214, "wing": 144, "other": 20}
 
 
