@@ -708,22 +708,40 @@ static_assert(sizeof(Stage32) == 80, "Stage32 is five 16-byte words");
 // add_tau_particle (absorption.cpp:225-247), FP32 form.  Returns false for a
 // pair whose smoothing sphere misses the sightline (absorption.cpp:232).
 // scale_nod (may be null) receives scale without the density factor.
-__device__ __forceinline__ bool stage32_setup(const LineParams &lp, const PairInput &in,
-                                              double bintov_d, Stage32 &st, float *scale_nod)
+// Float copies of the line constants the FP32 setup uses (once per sightline).
+struct Setup32 {
+    float bfac, voigt_fac, ampv, bintov;   // ampv = sigma_a / sqrt(pi) c / velfac
+    __device__ __forceinline__ Setup32(const LineParams &lp, double bintov_d)
+    {
+        bfac = (float)lp.bfac;
+        voigt_fac = (float)lp.voigt_fac;
+        ampv = (float)(lp.sigma_a / sqrt(PI_D) * LIGHT_KMS / lp.velfac);
+        bintov = (float)bintov_d;
+    }
+};
+
+// The quantities the FP32 form keeps in float (b, a, the amplitude) come
+// from float arithmetic (this GPU runs FP64 at 1/64 of the FP32 rate); the
+// particle's bin, its offset and the kernel support keep the reference's
+// double arithmetic, and so does the sub-sample count where the float ratio
+// lies within 1e-5 of one of its decision boundaries (the float ratio is
+// within 4e-7 of the double one).
+__device__ __forceinline__ bool stage32_setup(const LineParams &lp, const Setup32 &k,
+                                              const PairInput &in, double bintov_d,
+                                              Stage32 &st, float *scale_nod)
 {
     const double hh2 = (double)__fmul_rn(in.smooth, in.smooth);
     if (hh2 - in.dr2 <= 0)
         return false;
-    const double btherm = lp.bfac * sqrt((double)in.temp);
+    const float b = k.bfac * sqrtf(in.temp);
     const double vel = __dadd_rn(__dmul_rn(lp.velfac, (double)in.ppos), (double)in.pvel);
     const long long zmax = (long long)floor(vel / bintov_d);
     st.j0 = wrap_bin(zmax, lp.nbins);
     st.base0 = (float)((double)zmax * bintov_d - vel);   // FP64 offset of pixel zmax
-    const float b = (float)btherm;
     st.inv_b = 1.0f / b;
-    const double aa_d = lp.voigt_fac / btherm;
-    st.aa = (float)aa_d;
-    const bool wide = !(aa_d >= 0.0 && aa_d <= 0.1);
+    const float aa = k.voigt_fac * st.inv_b;
+    st.aa = aa;
+    const bool wide = !(aa >= 0.0f && aa <= 0.1f);
     const float vdr2 = (float)((lp.velfac * in.dr2) * lp.velfac);
     const float vsmooth = (float)(lp.velfac * (double)in.smooth);
     const float vhigh = (vsmooth * vsmooth > vdr2 ? sqrtf(vsmooth * vsmooth - vdr2) : 0.f);
@@ -767,25 +785,32 @@ __device__ __forceinline__ bool stage32_setup(const LineParams &lp, const PairIn
         const float umax = 3.f * fabsf(st.u1);
         st.vmp = fmaxf(3.34f * umax, umax + 6.5f);
     }
-    const double amp = lp.sigma_a / sqrt(PI_D) * (LIGHT_KMS / btherm);
-    // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov)
-    const double half_b = btherm / 2.;
-    double npd = 1.0;
-    if (!(bintov_d < half_b))
-        npd = 2 * ceil(bintov_d / half_b / 2) + 1.;
+    // tau_kern_outer sub-sampling: uniform for the pair (pixel width = bintov):
+    // 1 point if bintov < b/2, else 2 ceil(bintov / b) + 1
+    const float r = k.bintov * st.inv_b;
+    const float rn = (r + 12582912.0f) - 12582912.0f;   // nearest integer (r < 2^22)
+    double npd;
+    if (fabsf(r - 0.5f) < 1e-5f || (r >= 0.5f && r < 4e6f && fabsf(r - rn) < 1e-5f * r)) {
+        const double half_b = lp.bfac * sqrt((double)in.temp) / 2.;
+        npd = 1.0;
+        if (!(bintov_d < half_b))
+            npd = 2 * ceil(bintov_d / half_b / 2) + 1.;
+    } else {
+        npd = r < 0.5f ? 1.0 : 2.0 * (double)ceilf(r) + 1.0;
+    }
     if (!(npd <= MAX_SUBSAMPLES))
         npd = MAX_SUBSAMPLES + 1;   // flagged by the FP64 walk
     const int npoints = (int)npd;
     // Float node offsets keep ~1e-5 absolute accuracy only while |U_i| <= 256;
     // sub-sampled, very narrow or wide (a outside [0, 0.1]) profiles take the
     // FP64 walk.
-    const bool careful = wide || npoints > 8 || (double)vhigh > 256.0 * btherm;
-    double sc = amp / lp.velfac * (double)deltav;
+    const bool careful = wide || npoints > 8 || !(vhigh <= 256.0f * b);
+    float sc = k.ampv * st.inv_b * deltav;
     if (npoints > 1)
-        sc /= (npoints - 1);
+        sc /= (float)(npoints - 1);
     if (scale_nod)
-        *scale_nod = (float)sc;
-    st.scale = (float)(sc * (double)in.dens);
+        *scale_nod = sc;
+    st.scale = sc * in.dens;
     // Far-field tiles need a far wing that decreases with |V|: a positive
     // scale and non-negative multipole coefficients (the sum is then
     // increasing in 1/V^2).
@@ -1671,6 +1696,7 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
 {
     const int chunk = a.chunk;
     const float bintov_f = (float)bintov_d;
+    const Setup32 k32(a.lp, bintov_d);
     for (;;) {
         unsigned c = 0;
         if (lane == 0)
@@ -1706,14 +1732,14 @@ __device__ __forceinline__ void deposit_pairs32(const DepositArgs &a, int axis, 
                 s_stage_phase[w] = mphase ^ 1u;
             if (lane < n) {
                 Stage32 st;
-                if (!landed || !stage32_setup(a.lp, rec_input(r), bintov_d, st, nullptr))
+                if (!landed || !stage32_setup(a.lp, k32, rec_input(r), bintov_d, st, nullptr))
                     st.flags = STAGE_SKIP;
                 sw[lane] = st;
             }
         } else if (lane < n) {
             const PairInput in = load_pair(a.p, a.pl, cb + lane, axis, true, a.dev_err);
             Stage32 st;
-            if (!stage32_setup(a.lp, in, bintov_d, st, nullptr))
+            if (!stage32_setup(a.lp, k32, in, bintov_d, st, nullptr))
                 st.flags = STAGE_SKIP;
             sw[lane] = st;
         }
@@ -2484,6 +2510,7 @@ __global__ void __launch_bounds__(GRAD_THREADS, 1) grad_kernel(GradArgs a)
     const float tautail = (float)a.lp.tautail;
     const double bintov_d = a.lp.vbox / nbins;
     const float bintov_f = (float)bintov_d;
+    const Setup32 k32(a.lp, bintov_d);
     StageGrad *sw = reinterpret_cast<StageGrad *>(gsmem) + warp * GRAD_CHUNK;
     if (threadIdx.x == 0)
         s_ticket = atomicAdd(a.ticket, 1u);
@@ -2512,7 +2539,7 @@ __global__ void __launch_bounds__(GRAD_THREADS, 1) grad_kernel(GradArgs a)
                 g.temp = in.temp;
                 g.ip = a.pl.part[cb + lane];
                 g.pad = 0;
-                if (!stage32_setup(a.lp, in, bintov_d, g.s, &g.scale_nod))
+                if (!stage32_setup(a.lp, k32, in, bintov_d, g.s, &g.scale_nod))
                     g.s.flags = STAGE_SKIP;
                 sw[lane] = g;
             }
