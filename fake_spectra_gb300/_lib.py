@@ -34,6 +34,8 @@ EXPORTS = (
     "fsg_particle_interpolate_device",
     "fsg_spectra_batch_device",
     "fsg_tau_backward_device",
+    "fsg_tau_backward_reuse_device",
+    "fsg_context_search_generation",
     "fsg_build_pairs_device",
     "fsg_copy_pairs",
     "fsg_particle_interpolate_noalloc",
@@ -77,7 +79,7 @@ class Stats(ctypes.Structure):
                 ("launch_tuned", _c_i32), ("tune_ran", _c_i32), ("tune_candidates", _c_i32),
                 ("tune_sample_lines", _c_i32), ("launch_records", _c_i32),
                 ("tune_ms_default", _c_d), ("tune_ms_best", _c_d), ("ms_h2d", _c_d),
-                ("ms_d2h", _c_d), ("ms_flux", _c_d)]
+                ("ms_d2h", _c_d), ("ms_flux", _c_d), ("search_reused", _c_i32)]
 
 
 class TuneKey(ctypes.Structure):
@@ -156,6 +158,11 @@ def load(path=None):
         L.fsg_tau_backward_device.argtypes = ([_p, _c_int, _c_int] + [_c_d] * 8 + [_p] * 5 +
                                               [_c_i64, _p, _p, _c_i32, _p, _p, _p, _p, _p,
                                                _c_size])
+        L.fsg_tau_backward_reuse_device.argtypes = ([_p, ctypes.c_uint64, _c_int, _c_int] +
+                                                    [_c_d] * 8 + [_p] * 5 +
+                                                    [_c_i64, _p, _p, _c_i32, _p, _p, _p, _p,
+                                                     _p, _c_size])
+        L.fsg_context_search_generation.argtypes = [_p, ctypes.POINTER(ctypes.c_uint64)]
         L.fsg_build_pairs_device.argtypes = [_p, _c_d, _p, _p, _c_i64, _p, _p, _c_i32,
                                              ctypes.POINTER(_c_i64), _p, _c_size]
         L.fsg_copy_pairs.argtypes = [_p, _p, _p, _p, _c_int, _p, _c_size]
@@ -241,6 +248,13 @@ class Context:
         self._lib.fsg_context_stats(self._h, ctypes.byref(s))
         return _stats_dict(s)
 
+    def search_generation(self):
+        """The context's sightline-search generation (grows with every search)."""
+        g = ctypes.c_uint64(0)
+        if load().fsg_context_search_generation(self.handle, ctypes.byref(g)) != FSG_OK:
+            raise RuntimeError("fsg_context_search_generation failed")
+        return int(g.value)
+
     def close(self):
         if self._h:
             self._lib.fsg_context_destroy(self._h)
@@ -279,7 +293,8 @@ def _stats_dict(s):
                      "sample_lines": int(s.tune_sample_lines),
                      "ms_default": float(s.tune_ms_default),
                      "ms_best": float(s.tune_ms_best)},
-            "ms_h2d": float(s.ms_h2d), "ms_d2h": float(s.ms_d2h), "ms_flux": float(s.ms_flux)}
+            "ms_h2d": float(s.ms_h2d), "ms_d2h": float(s.ms_d2h), "ms_flux": float(s.ms_flux),
+            "search_reused": int(s.search_reused)}
 
 
 def fma_peak_tflops(precision="fp32"):

@@ -4,9 +4,10 @@
 tau (float64, [nlos, nbins]) differentiable with respect to `dens`, `temp` and
 `vel` (the line-of-sight component).  The forward is the FP32 deposit kernel,
 the backward the hand-written backward kernel (include/fsg.h,
-fsg_tau_backward_device), which recomputes the sightline search and the
-profiles instead of storing them.  Positions and smoothing lengths are inputs
-without gradients.
+fsg_tau_backward_reuse_device), which reuses the forward's sightline search
+when it is still the context's last one (torch's version counters guard the
+saved positions and smoothing lengths) and recomputes the profiles instead of
+storing them.  Positions and smoothing lengths are inputs without gradients.
 """
 import torch
 
@@ -20,6 +21,7 @@ class _ParticleTau(torch.autograd.Function):
                                                  precision="fp32")
         fctx.ctx = ctx
         fctx.args = args
+        fctx.generation = ctx.search_generation()
         fctx.axis = axis
         fctx.cofm = cofm
         fctx.save_for_backward(pos, vel, dens, temp, hh)
@@ -30,7 +32,8 @@ class _ParticleTau(torch.autograd.Function):
         pos, vel, dens, temp, hh = fctx.saved_tensors
         gd, gt, gv = interp.tau_backward_device(fctx.ctx, *fctx.args[1:], pos, vel, dens, temp, hh,
                                                 fctx.axis, fctx.cofm,
-                                                grad_tau.to(torch.float64))
+                                                grad_tau.to(torch.float64),
+                                                generation=fctx.generation)
         return None, None, None, gv, gd, gt, None, None, None
 
 

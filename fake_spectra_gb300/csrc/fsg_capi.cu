@@ -122,6 +122,18 @@ struct fsg_context {
     int nlos = 0;
     long long npairs = 0;
     LineTables tables{};
+    // The last sightline search: a generation count and its inputs.  A
+    // backward call may reuse its pair lists only when all of them match
+    // (build_tables clears the record; search_pairs writes it when it is done).
+    unsigned long long search_gen = 0;
+    struct SearchRecord {
+        const void *pos = nullptr, *hh = nullptr;
+        long long npart = -1;
+        int nlos = -1;
+        double box = 0.0;
+        unsigned long long lines = 0;   // hash of the axis and cofm arrays
+    } search_rec;
+    unsigned long long lines_hash = 0;   // of the tables build_tables last built
     fsg_stats stats{};
 
     void *ensure(DevBuf &b, size_t bytes)
@@ -208,8 +220,26 @@ void validate_common(int nbins, int kernel, double box, int64_t npart, int32_t n
 }
 
 // 1. sightline tables
+// FNV-1a over the sightline arrays (identifies the tables a search used).
+unsigned long long lines_hash_of(const int32_t *axis, const double *cofm, int nlos)
+{
+    unsigned long long h = 1469598103934665603ull;
+    const auto mix = [&](const void *p, size_t n) {
+        const unsigned char *b = (const unsigned char *)p;
+        for (size_t i = 0; i < n; i++) {
+            h ^= b[i];
+            h *= 1099511628211ull;
+        }
+    };
+    mix(axis, sizeof(int32_t) * (size_t)nlos);
+    mix(cofm, sizeof(double) * 3 * (size_t)nlos);
+    return h;
+}
+
 void build_tables(fsg_context *c, const int32_t *axis, const double *cofm, int nlos, double box)
 {
+    c->search_rec = fsg_context::SearchRecord{};
+    c->lines_hash = lines_hash_of(axis, cofm, nlos);
     std::vector<double> key(nlos), second(nlos);
     std::vector<int> grp_lines[3];
     for (int i = 0; i < nlos; i++) {
@@ -360,6 +390,9 @@ void search_pairs(fsg_context *c, const Particles &p, int nlos)
     if (h_err)
         fail(FSG_ERR_DEVICE, "pair search reported device error bits 0x%x (%s)", h_err,
              deverr_text(h_err).c_str());
+    c->search_gen++;
+    c->search_rec = fsg_context::SearchRecord{p.pos, p.hh, p.n, nlos, c->tables.box,
+                                              c->lines_hash};
 }
 
 // _near_lines (py_module.cpp:25-99): ascending indices of the particles within
@@ -1584,15 +1617,14 @@ int fsg_spectra_batch_device(fsg_context *ctx, int nbins, int kernel, double box
     }
 }
 
-int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
-                            double atime, double lambda, double gamma, double fosc,
-                            double amumass, double tautail, const float *pos, const float *vel,
-                            const float *dens, const float *temp, const float *h, int64_t npart,
-                            const int32_t *axis, const double *cofm, int32_t nlos,
-                            const double *grad_tau, float *grad_dens, float *grad_temp,
-                            float *grad_vel, char *errbuf, size_t errlen)
+static int tau_backward(fsg_context *ctx, const unsigned long long *reuse_gen, int nbins,
+                        int kernel, double box, double velfac, double lambda, double gamma,
+                        double fosc, double amumass, double tautail, const float *pos,
+                        const float *vel, const float *dens, const float *temp, const float *h,
+                        int64_t npart, const int32_t *axis, const double *cofm, int32_t nlos,
+                        const double *grad_tau, float *grad_dens, float *grad_temp,
+                        float *grad_vel, char *errbuf, size_t errlen)
 {
-    (void)atime;
     try {
         if (!ctx)
             fail(FSG_ERR_VALUE, "ctx is NULL");
@@ -1600,9 +1632,16 @@ int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box,
         if (!grad_tau || !grad_dens || !grad_temp || !grad_vel)
             fail(FSG_ERR_VALUE, "gradient buffers must not be NULL");
         cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice");
-        build_tables(ctx, axis, cofm, nlos, box);
         Particles p{pos, vel, dens, temp, h, (long long)npart};
-        search_pairs(ctx, p, nlos);
+        const fsg_context::SearchRecord &r = ctx->search_rec;
+        const bool reuse = reuse_gen && *reuse_gen == ctx->search_gen && r.pos == pos &&
+                           r.hh == h && r.npart == (long long)npart && r.nlos == nlos &&
+                           r.box == box && r.lines == lines_hash_of(axis, cofm, nlos);
+        ctx->stats.search_reused = reuse ? 1 : 0;
+        if (!reuse) {
+            build_tables(ctx, axis, cofm, nlos, box);
+            search_pairs(ctx, p, nlos);
+        }
         if (nlos == 0 || nbins == 0 || ctx->npairs == 0)
             return FSG_OK;
         LineParams lp = make_line_params(1, nbins, kernel, box, velfac, lambda, gamma, fosc,
@@ -1637,6 +1676,44 @@ int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box,
     } catch (const FsgError &e) {
         return report(e, errbuf, errlen);
     }
+}
+
+int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box, double velfac,
+                            double atime, double lambda, double gamma, double fosc,
+                            double amumass, double tautail, const float *pos, const float *vel,
+                            const float *dens, const float *temp, const float *h, int64_t npart,
+                            const int32_t *axis, const double *cofm, int32_t nlos,
+                            const double *grad_tau, float *grad_dens, float *grad_temp,
+                            float *grad_vel, char *errbuf, size_t errlen)
+{
+    (void)atime;
+    return tau_backward(ctx, nullptr, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
+                        tautail, pos, vel, dens, temp, h, npart, axis, cofm, nlos, grad_tau,
+                        grad_dens, grad_temp, grad_vel, errbuf, errlen);
+}
+
+int fsg_tau_backward_reuse_device(fsg_context *ctx, uint64_t generation, int nbins, int kernel,
+                                  double box, double velfac, double atime, double lambda,
+                                  double gamma, double fosc, double amumass, double tautail,
+                                  const float *pos, const float *vel, const float *dens,
+                                  const float *temp, const float *h, int64_t npart,
+                                  const int32_t *axis, const double *cofm, int32_t nlos,
+                                  const double *grad_tau, float *grad_dens, float *grad_temp,
+                                  float *grad_vel, char *errbuf, size_t errlen)
+{
+    (void)atime;
+    const unsigned long long g = generation;
+    return tau_backward(ctx, &g, nbins, kernel, box, velfac, lambda, gamma, fosc, amumass,
+                        tautail, pos, vel, dens, temp, h, npart, axis, cofm, nlos, grad_tau,
+                        grad_dens, grad_temp, grad_vel, errbuf, errlen);
+}
+
+int fsg_context_search_generation(const fsg_context *ctx, uint64_t *generation)
+{
+    if (!ctx || !generation)
+        return FSG_ERR_VALUE;
+    *generation = ctx->search_gen;
+    return FSG_OK;
 }
 
 int fsg_build_pairs_device(fsg_context *ctx, double box, const float *pos, const float *h,

@@ -118,8 +118,13 @@ def spectra_batch_device(ctx, nbins, kernel, box, velfac, atime, tautail, pos, v
 
 
 def tau_backward_device(ctx, nbins, kernel, box, velfac, atime, lam, gamma, fosc, amumass,
-                        tautail, pos, vel, dens, temp, h, axis, cofm, grad_tau):
-    """Gradients (d_dens, d_temp, d_vel) of L from dL/dtau, FP32, new float32 tensors."""
+                        tautail, pos, vel, dens, temp, h, axis, cofm, grad_tau,
+                        generation=None):
+    """Gradients (d_dens, d_temp, d_vel) of L from dL/dtau, FP32, new float32 tensors.
+    With `generation` (ctx.search_generation() right after the forward call on
+    the same pos, h, axis and cofm, whose contents the caller has not changed)
+    the forward's sightline search is reused when it is still the context's
+    last one."""
     import torch
     axis, cofm = _host_tables(axis, cofm)
     gd = torch.zeros_like(dens)
@@ -129,14 +134,18 @@ def tau_backward_device(ctx, nbins, kernel, box, velfac, atime, lam, gamma, fosc
     _bind_stream(ctx)
     eb = _lib.errbuf()
     L = _lib.load()
-    rc = L.fsg_tau_backward_device(
-        ctx.handle, int(nbins), int(kernel), float(box), float(velfac), float(atime), float(lam),
-        float(gamma), float(fosc), float(amumass), float(tautail), _dptr(pos, "float32", "pos"),
-        _dptr(vel, "float32", "vel"), _dptr(dens, "float32", "dens"),
-        _dptr(temp, "float32", "temp"), _dptr(h, "float32", "h"), int(pos.shape[0]),
-        axis.ctypes.data_as(ctypes.c_void_p), cofm.ctypes.data_as(ctypes.c_void_p),
-        int(axis.shape[0]), _dptr(grad_tau, "float64", "grad_tau"), _dptr(gd, "float32", "gd"),
-        _dptr(gt, "float32", "gt"), _dptr(gv, "float32", "gv"), eb, 512)
+    tail = (int(nbins), int(kernel), float(box), float(velfac), float(atime), float(lam),
+            float(gamma), float(fosc), float(amumass), float(tautail),
+            _dptr(pos, "float32", "pos"), _dptr(vel, "float32", "vel"),
+            _dptr(dens, "float32", "dens"), _dptr(temp, "float32", "temp"),
+            _dptr(h, "float32", "h"), int(pos.shape[0]), axis.ctypes.data_as(ctypes.c_void_p),
+            cofm.ctypes.data_as(ctypes.c_void_p), int(axis.shape[0]),
+            _dptr(grad_tau, "float64", "grad_tau"), _dptr(gd, "float32", "gd"),
+            _dptr(gt, "float32", "gt"), _dptr(gv, "float32", "gv"), eb, 512)
+    if generation is None:
+        rc = L.fsg_tau_backward_device(ctx.handle, *tail)
+    else:
+        rc = L.fsg_tau_backward_reuse_device(ctx.handle, int(generation), *tail)
     _lib.raise_for(rc, eb.value.decode(errors="replace"))
     return gd, gt, gv
 

@@ -97,6 +97,7 @@ typedef struct {
      * device->host copy of the output of the last call, device time */
     double ms_h2d, ms_d2h;
     double ms_flux;              /* device time of the last flux-statistics call's kernels */
+    int32_t search_reused;       /* 1: the last backward call reused the last search */
 } fsg_stats;
 
 typedef struct fsg_context fsg_context;
@@ -282,6 +283,26 @@ int fsg_tau_backward_device(fsg_context *ctx, int nbins, int kernel, double box,
                             const int32_t *axis, const double *cofm, int32_t nlos,
                             const double *grad_tau, float *grad_dens, float *grad_temp,
                             float *grad_vel, char *errbuf, size_t errlen);
+
+/* fsg_tau_backward_device that reuses the sightline search of the forward call
+ * it follows: when `generation` is the context's search generation
+ * (fsg_context_search_generation right after that call) and pos, h, npart,
+ * nlos, box and the axis/cofm contents are those the search used, the pair
+ * lists are taken as they are (the caller must not have changed the contents
+ * of pos and h in between); otherwise the search runs again.  Same arguments
+ * and results as fsg_tau_backward_device. */
+int fsg_tau_backward_reuse_device(fsg_context *ctx, uint64_t generation, int nbins, int kernel,
+                                  double box, double velfac, double atime, double lambda,
+                                  double gamma, double fosc, double amumass, double tautail,
+                                  const float *pos, const float *vel, const float *dens,
+                                  const float *temp, const float *h, int64_t npart,
+                                  const int32_t *axis, const double *cofm, int32_t nlos,
+                                  const double *grad_tau, float *grad_dens, float *grad_temp,
+                                  float *grad_vel, char *errbuf, size_t errlen);
+
+/* The context's sightline-search generation: it grows by one with every
+ * search the context runs. */
+int fsg_context_search_generation(const fsg_context *ctx, uint64_t *generation);
 
 /* Copy the context's pair lists to HOST buffers as CSR by sightline:
  * offsets[nlos+1], part[npairs], dr2[npairs].  Within a sightline the pairs

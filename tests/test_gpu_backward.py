@@ -227,3 +227,40 @@ def test_backward_config4_against_oracle_fd(ctx, port):
           "sub-sample count moved by the step); relative error median %.2e, 99th pct %.2e"
           % (checked, 3 * len(chosen), skipped, np.median(rel), np.percentile(rel, 99)))
     assert checked >= 0.9 * 3 * len(chosen)
+
+
+def test_backward_reuses_the_forward_search(ctx):
+    """The autograd backward reuses the forward's sightline search (the
+    context's search generation and the search inputs match), and gives the
+    gradients of the backward that searches again, up to the order of its
+    float atomics.  After another search on the context the reuse entry
+    searches again."""
+    import torch
+    from fake_spectra_gb300 import interp as I
+    w = small_workload()
+    target = np.exp(-np.full((len(w.axis), w.nbins), 0.3))
+    gd, gt, gv = gpu_grads(ctx, w, target)
+    assert ctx.stats()["search_reused"] == 1
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    t = synth.LYA
+    args = (w.nbins, w.kernel, w.box, w.velfac, w.atime, t.lambda_cm, t.gamma, t.fosc,
+            t.amumass, w.tautail)
+    pos, vel, dens, temp, hh = T(w.pos), T(w.vel), T(w.dens["HI"]), T(w.temp), T(w.hh)
+    tau = I.particle_interpolate_device(ctx, 1, *args, pos, vel, dens, temp, hh, w.axis, w.cofm,
+                                        precision="fp32")
+    F = torch.exp(-tau)
+    grad_tau = -2.0 * (F - T(target)) * F
+    gen = ctx.search_generation()
+    # an unrelated search on the same context in between: the reuse entry must search again
+    I.particle_interpolate_device(ctx, 1, *args, pos + 1.0, vel, dens, temp, hh, w.axis,
+                                  w.cofm, precision="fp32")
+    r = I.tau_backward_device(ctx, *args, pos, vel, dens, temp, hh, w.axis, w.cofm, grad_tau,
+                              generation=gen)
+    assert ctx.stats()["search_reused"] == 0
+    fresh = I.tau_backward_device(ctx, *args, pos, vel, dens, temp, hh, w.axis, w.cofm, grad_tau)
+    for got, want in zip((gd, gt, gv), fresh):
+        want = want.cpu().numpy().astype(np.float64)
+        np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-6 * np.abs(want).max())
+    for got, want in zip(r, fresh):
+        np.testing.assert_allclose(got.cpu().numpy(), want.cpu().numpy(), rtol=1e-4,
+                                   atol=1e-6 * float(want.abs().max()))
